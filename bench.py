@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Cost+gradient throughput of the B-spline registration path on GB300.
+
+Workload (default): the 3D single-pair configuration — 192x192x128 float32
+blob phantoms (40 blobs, sigma U(4,16), amplitude U(50,200), N(0,2) noise),
+the moving volume warped by a random cubic B-spline field (knot spacing 8,
+coefficients N(0,2) clipped to +-4), joint mean-0/sigma-1 normalisation as
+the registration driver applies it, then repeated evaluations of SSD +
+divcurl(weight 10) cost and gradient at fixed coefficients (spline rate 8,
+bspline:d=3 interpolation).  A "step" is one cost+gradient evaluation.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` is device-timed Mvoxel/s with inputs resident in HBM (L2 flushed
+between steps, flush excluded); `e2e` is the same metric through the C ABI
+with host parameter/gradient buffers (pinned), copies included.  The
+reference arm times the CPU restatement of the reference algorithm (the
+oracle; the reference itself cannot be built here) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cost+grad Mvoxel/s (3D SSD/NCC) & batched pairs/s vs plain GPU, grad err ≤1e-4"
+
+WORKLOADS = {
+    "3d_ssd_192x192x128": dict(size=(192, 192, 128), nblobs=40, sigma=(4.0, 16.0), rate=8.0, wsigma=2.0,
+                               wclip=4.0, cost="ssd", penalty=10.0, bias=None, seed=2000),
+    "3d_ncc_256x256x256": dict(size=(256, 256, 256), nblobs=40, sigma=(4.0, 16.0), rate=5.0, wsigma=2.0,
+                               wclip=4.0, cost="ncc", penalty=5.0, bias=0.1, seed=3000),
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload(name, device):
+    """Generate (moving, reference, params) on the host; the deformation is
+    applied with this library's own warp."""
+    import mia_gb300 as M
+    from mia_gb300 import synth
+    w = WORKLOADS[name]
+    size = w["size"]
+    shape = size[::-1]
+    ref = synth.blob_phantom(shape, w["nblobs"], sigma=w["sigma"], seed=w["seed"])
+    lv = M.Level(size, rate=w["rate"], device=device)
+    lv.set_images(ref, ref)
+    true_p = synth.spline_params(lv.nparams // 3, 3, w["wsigma"], w["wclip"], seed=w["seed"] + 1)
+    mov = lv.warp(true_p)
+    lv.close()
+    if w["bias"]:
+        mov = (mov * synth.bias_field(shape, w["bias"], seed=w["seed"] + 2)).astype(np.float32)
+    # FScaleFilterCreator (mia/template/nonrigidregister.cxx:147-184)
+    a = mov.astype(np.float64).ravel()
+    b = ref.astype(np.float64).ravel()
+    n = 2 * a.size
+    s = a.sum() + b.sum()
+    s2 = (a * a).sum() + (b * b).sum()
+    mean = s / n
+    sig = np.sqrt((s2 - s * s / n) / (n - 1))
+    mov = ((mov - mean) / sig).astype(np.float32)
+    ref = ((ref - mean) / sig).astype(np.float32)
+    params = 0.5 * synth.spline_params(len(true_p) // 3, 3, w["wsigma"], w["wclip"], seed=w["seed"] + 3)
+    return w, mov, ref, params
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """per-launch DRAM bytes of `kernel` from the committed ncu summary"""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        v = d.get(kernel)
+        if v:
+            return float(v["bytes_per_launch"])
+    return None
+
+
+def cpu_baseline(w, mov, ref, params, seconds, threads):
+    from oracle import oracle as O
+    size = w["size"]
+    lv = O.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], threads=threads)
+    lv.set_images(mov, ref)
+    n = 0
+    t0 = time.perf_counter()
+    res = None
+    while True:
+        res = lv.evaluate(params)
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    N = int(np.prod(size))
+    return N * n / dt / 1e6, n, dt, res
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    name = args.workload
+    w = WORKLOADS[name]
+    # inputs generated on the host only (the reference arm uses no GPU code)
+    from mia_gb300 import synth
+    from oracle import oracle as O
+    size = w["size"]
+    shape = size[::-1]
+    ref = synth.blob_phantom(shape, w["nblobs"], sigma=w["sigma"], seed=w["seed"])
+    threads = os.cpu_count() or 1
+    lvw = O.Level(size, rate=w["rate"], threads=threads)
+    lvw.set_images(ref, ref)
+    true_p = synth.spline_params(lvw.nparams // 3, 3, w["wsigma"], w["wclip"], seed=w["seed"] + 1)
+    mov = lvw.warp(true_p)
+    params = 0.5 * synth.spline_params(len(true_p) // 3, 3, w["wsigma"], w["wclip"], seed=w["seed"] + 3)
+    lv = O.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], threads=threads)
+    lv.set_images(mov, ref)
+    for _ in range(args.warmup):
+        lv.evaluate(params)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lv.evaluate(params)
+    dt = time.perf_counter() - t0
+    N = int(np.prod(size))
+    v = N * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mvoxel/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "size": list(size), "rate": w["rate"], "cost": w["cost"],
+                   "divcurl_weight": w["penalty"]},
+        "cpu_baseline": {"value": v, "unit": "Mvoxel/s", "cores": threads, "kind": "port",
+                         "sample": "%d full evaluations of %s" % (args.steps, "x".join(map(str, size)))},
+        "e2e": {"value": v, "unit": "Mvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import mia_gb300 as M
+    name = args.workload
+    w, mov, ref, params = make_workload(name, local)
+    size = w["size"]
+    N = int(np.prod(size))
+    lv = M.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], device=local)
+    lv.set_images(mov, ref)
+    nparams = lv.nparams
+    dev = torch.device("cuda", local)
+    p_d = torch.from_numpy(params).to(dev)
+    g_d = torch.empty(nparams, dtype=torch.float64, device=dev)
+    c_d = torch.empty(2, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    lv.set_timing(True)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
+        lv.sync()
+    launches0 = M.lib().mgr_kernel_launch_count()
+    per = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
+            per.append(lv.kernel_times())
+        lv.sync()
+        torch.cuda.synchronize()
+    barrier()
+    launches = M.lib().mgr_kernel_launch_count() - launches0
+    per = np.array(per)
+    t_step = per[:, 3].mean() / 1e3
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = ws * N / t_step / 1e6
+
+    # end to end through the C ABI: host (pinned) params in, gradient out
+    hp = torch.from_numpy(params).pin_memory().numpy()
+    hg = torch.empty(nparams, dtype=torch.float64).pin_memory().numpy()
+    lv.set_timing(False)
+    for _ in range(max(1, args.warmup)):
+        lv.evaluate_total(hp, hg)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lv.evaluate_total(hp, hg)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_step = float(np.mean(e2e_t))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+
+    if rank != 0:
+        return 0
+    D, C = 3, nparams // 3
+    b_eval = 8.0 * N + 12.0 * D * C
+    b_warp = 8.0 * N + 4.0 * N + 8.0 * D * C      # M and R read, W written, params read
+    peak, peak_kind = measured_peaks()
+    t_warp = per[:, 0].mean() / 1e3
+    traffic = profile_traffic("k_warp<3>")
+    roof = {"bound": "hbm", "kernel": "k_warp<3>", "achieved": b_warp / t_warp / 1e9, "peak": peak,
+            "unit": "GB/s", "frac": b_warp / t_warp / 1e9 / peak, "traffic": traffic,
+            "peak_kind": peak_kind, "algorithmic_bytes": b_warp}
+    eval_roof = {"achieved": b_eval / t_step / 1e9, "frac": b_eval / t_step / 1e9 / peak,
+                 "algorithmic_bytes": b_eval, "unit": "GB/s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mvoxel/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "size": list(size), "rate": w["rate"], "cost": w["cost"],
+                   "divcurl_weight": w["penalty"], "coefficients": list(lv.csize), "path": "split",
+                   "l2": "flushed between steps (256 MiB write), flush excluded from timing",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "e2e": {"value": ws * N / e2e_step / 1e6, "unit": "Mvoxel/s", "h2d_bytes_per_step": nparams * 8,
+                "d2h_bytes_per_step": nparams * 8 + 16},
+        "gpu_launches": int(launches),
+        "kernel_ms": {"warp": float(per[:, 0].mean()), "adjoint": float(per[:, 1].mean()),
+                      "gather_penalty": float(per[:, 2].mean())},
+        "roofline": roof,
+        "eval_roofline": eval_roof,
+        "clocks": clk.summary(),
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, dt, res = cpu_baseline(w, mov, ref, params, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "Mvoxel/s", "cores": threads, "kind": "port",
+                                "sample": "%d full %s evaluations in %.1f s" % (n, "x".join(map(str, size)), dt)}
+        ci, cp, gi, gp, gt = lv.evaluate(params)
+        oi, op, ogi, ogp = res
+        line["parity"] = {
+            "cost_image_rel": abs(ci - oi) / abs(oi), "cost_penalty_rel": abs(cp - op) / abs(op),
+            "grad_image_rel_l2": float(np.linalg.norm(gi - ogi) / np.linalg.norm(ogi)),
+            "grad_penalty_rel_l2": float(np.linalg.norm(gp - ogp) / np.linalg.norm(ogp)),
+            "against": "oracle, reference precision"}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="3d_ssd_192x192x128", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

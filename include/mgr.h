@@ -1,0 +1,152 @@
+/*
+ * mgr.h — C ABI of libmgr.so: GB300 (sm_103a) implementation of MIA's
+ * B-spline nonrigid-registration cost+gradient path.
+ *
+ * One `mgr_level` holds one image pair at one resolution level on one GPU
+ * stream: the `spline` transformation (bspline:d=3 coefficients), the
+ * `image` full cost with the `ssd` or `ncc` image cost, and the optional
+ * `divcurl` spline penalty.  Every call returns an mgr_status; on failure
+ * mgr_last_error() returns a message for the calling thread.  No call throws
+ * and no call falls back to the CPU: without a usable GPU the calls fail
+ * with MGR_ERR_CUDA.
+ *
+ * Parameter vectors are laid out as MIA's CDoubleVector for a spline
+ * transformation: one (x, y[, z]) double triple per coefficient, x fastest
+ * over the coefficient grid (mia/3d/transform/spline.cc:329-358).  Images
+ * are float, x fastest.  Host pointers are copied synchronously; the
+ * *_device variants take device pointers, run asynchronously on the level's
+ * stream and return before completion.
+ */
+#ifndef MGR_H
+#define MGR_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MGR_OK = 0,
+    MGR_ERR_ARG = 1,      /* invalid argument (std::invalid_argument in MIA) */
+    MGR_ERR_CUDA = 2,     /* CUDA runtime failure or no GPU */
+    MGR_ERR_OOM = 3,      /* device allocation failed */
+    MGR_ERR_TIMEOUT = 4,  /* a bounded device wait gave up */
+    MGR_ERR_STATE = 5     /* call out of order (e.g. evaluate before set_images) */
+} mgr_status;
+
+enum { MGR_COST_SSD = 0, MGR_COST_NCC = 1 };
+
+/* Evaluation strategy of the image term.
+   MGR_PATH_SPLIT: warp kernel (displacement + tricubic sample + cost sums),
+                   then one fused gradient/force/adjoint kernel, then the
+                   per-coefficient gather (default, fastest).
+   MGR_PATH_PLAIN: one kernel per reference step (dense grid, warp, image
+                   gradient, force, separable translate, value) — the plain
+                   per-pair drop-in used as the comparison baseline. */
+enum { MGR_PATH_SPLIT = 0, MGR_PATH_PLAIN = 1 };
+
+/* Level description; field names follow the plugin parameters:
+   spline:rate, image:cost/weight, ssd:norm, divcurl:weight/div/curl/norm. */
+typedef struct {
+    int    dim;          /* 2 or 3 */
+    int    size[3];      /* image size (x,y,z); size[2] ignored for dim 2 */
+    int    csize[3];     /* coefficient grid incl. border; 0 = derive from rate */
+    float  rate[3];      /* spline `rate` (coefficient spacing), >= 1 */
+    int    cost;         /* MGR_COST_SSD / MGR_COST_NCC */
+    int    ssd_norm;     /* ssd `norm` (divide by the number of voxels) */
+    double cost_weight;  /* image full-cost `weight` */
+    int    has_penalty;  /* 1 if the transformation carries a divcurl penalty */
+    double pen_weight;   /* divcurl `weight` */
+    double pen_div;      /* divcurl `div` */
+    double pen_curl;     /* divcurl `curl` */
+    int    pen_norm;     /* divcurl `norm` (divide by the image volume) */
+} mgr_level_desc;
+
+typedef struct mgr_level mgr_level;
+
+/* Thread-local message of the last failed call on this thread. */
+const char *mgr_last_error(void);
+
+/* Replaces: C3DSplineTransformation ctor + reinit
+   (mia/3d/transform/spline.cc:102-147, 224-275), the divcurl penalty
+   initialize (mia/3d/splinetransformpenalty.cc:43-49) and the image full
+   cost set_size (mia/3d/fullcost/image.cc:80-98).  `stream` is a
+   cudaStream_t or NULL for a stream owned by the level. */
+mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream,
+                            mgr_level **out);
+mgr_status mgr_level_destroy(mgr_level *lvl);
+
+/* Coefficient grid and number of parameters (degrees_of_freedom,
+   mia/3d/transform/spline.cc:414-418). */
+mgr_status mgr_level_csize(const mgr_level *lvl, int csize[3], size_t *nparams);
+
+/* Replaces: C3DImageFullCost::do_reinit + TCost::set_reference
+   (mia/3d/fullcost/image.cc:112-128, mia/core/cost.cxx:43-48) and the
+   interpolator prefilter (mia/3d/interpolator.cxx:98-164), done once here
+   instead of on every warp.  Host pointers, `size` voxels each. */
+mgr_status mgr_level_set_images(mgr_level *lvl, const float *src, const float *ref);
+mgr_status mgr_level_set_images_device(mgr_level *lvl, const float *d_src, const float *d_ref);
+
+/* Replaces: TNonrigRegGradientProblem::evaluate_fdf
+   (mia/template/nonrigidregister.cxx:415-439) = TFullCost::evaluate of the
+   image cost (C3DImageFullCost::do_evaluate, mia/3d/fullcost/image.cc:67-78:
+   warp, evaluate_force, translate, value) plus the penalty's
+   value_and_gradient (mia/3d/splinetransformpenalty.cc:60-71, with its
+   reference sign).  Any output pointer may be NULL.
+   grad_total = grad_image + grad_penalty, as evaluate_fdf returns it. */
+mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad_total,
+                              double *grad_image, double *grad_penalty,
+                              double *cost_image, double *cost_penalty);
+
+/* Device variant: params / grad_total are device pointers (nparams doubles),
+   d_costs receives {cost_image, cost_penalty} (2 doubles, device). */
+mgr_status mgr_level_evaluate_device(mgr_level *lvl, const double *d_params,
+                                     double *d_grad_total, double *d_costs);
+
+/* Replaces: TNonrigRegGradientProblem::do_f (nonrigidregister.cxx:376-396):
+   C3DImageFullCost::do_value + get_energy_penalty (C3DPPDivcurlMatrix
+   operator*, mia/3d/ppmatrix.cc:292-361). */
+mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_image,
+                           double *cost_penalty);
+
+/* Replaces: Transformation::operator()(image) for the spline transformation
+   (mia/3d/transform.cc:280-323) — the warped moving image. */
+mgr_status mgr_level_warp(mgr_level *lvl, const double *params, float *out);
+
+/* Replaces: TCost::evaluate_force (mia/core/cost.cxx:37-41) on the warped
+   image; writes dim floats per voxel and returns the force-pass cost. */
+mgr_status mgr_level_force(mgr_level *lvl, const double *params, float *force,
+                           double *cost);
+
+/* Replaces: C3DSplineTransformation::translate / C2DSplineTransformation::
+   translate (mia/3d/transform/spline.cc:731-791,
+   mia/2d/transform/spline.cc:540-576) for a caller-supplied force field. */
+mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad);
+
+/* Select the evaluation strategy (MGR_PATH_*) and, for MGR_PATH_SPLIT, the
+   tile shape (0 = autotuned default).  Has no counterpart in the
+   reference: it chooses between implementations of the same result. */
+mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z);
+
+/* Kernel timing for profiling: with `enable` set, every evaluation records
+   CUDA events around its kernels on the level's stream.
+   mgr_level_kernel_times waits for the last evaluation and writes the
+   device time in milliseconds of its kernels: ms[0] warp, ms[1]
+   gradient/force/adjoint, ms[2] gather+penalty, ms[3] the whole image and
+   penalty term (plain path: ms[3] only).  Has no counterpart in the
+   reference (it replaces its optional TRACE logging of timings). */
+mgr_status mgr_level_set_timing(mgr_level *lvl, int enable);
+mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4]);
+
+/* Wait for all work queued on the level's stream. */
+mgr_status mgr_level_sync(mgr_level *lvl);
+
+/* Number of kernels this library has launched in the calling process
+   (for launch accounting in benchmarks). */
+unsigned long long mgr_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,87 @@
+"""ctypes binding of libmgr.so (the C ABI declared in include/mgr.h).
+
+The library is loaded from this package directory; there is no fallback.
+If libmgr.so is missing or cannot be loaded, ``lib()`` raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmgr.so")
+
+MGR_OK, MGR_ERR_ARG, MGR_ERR_CUDA, MGR_ERR_OOM, MGR_ERR_TIMEOUT, MGR_ERR_STATE = range(6)
+COST_SSD, COST_NCC = 0, 1
+PATH_SPLIT, PATH_PLAIN = 0, 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+# every exported entry point of include/mgr.h with (restype, argtypes)
+SIGNATURES = {
+    "mgr_last_error": (ctypes.c_char_p, []),
+    "mgr_kernel_launch_count": (ctypes.c_ulonglong, []),
+    "mgr_level_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
+    "mgr_level_destroy": (ctypes.c_int, [_vp]),
+    "mgr_level_csize": (ctypes.c_int, [_vp, _ip, ctypes.POINTER(ctypes.c_size_t)]),
+    "mgr_level_set_images": (ctypes.c_int, [_vp, _fp, _fp]),
+    "mgr_level_set_images_device": (ctypes.c_int, [_vp, _vp, _vp]),
+    "mgr_level_evaluate": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "mgr_level_evaluate_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "mgr_level_value": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "mgr_level_warp": (ctypes.c_int, [_vp, _dp, _fp]),
+    "mgr_level_force": (ctypes.c_int, [_vp, _dp, _fp, _dp]),
+    "mgr_level_translate": (ctypes.c_int, [_vp, _fp, _dp]),
+    "mgr_level_set_path": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "mgr_level_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "mgr_level_kernel_times": (ctypes.c_int, [_vp, _dp]),
+    "mgr_level_sync": (ctypes.c_int, [_vp]),
+}
+
+
+class LevelDesc(ctypes.Structure):
+    """mgr_level_desc"""
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("size", ctypes.c_int * 3),
+        ("csize", ctypes.c_int * 3),
+        ("rate", ctypes.c_float * 3),
+        ("cost", ctypes.c_int),
+        ("ssd_norm", ctypes.c_int),
+        ("cost_weight", ctypes.c_double),
+        ("has_penalty", ctypes.c_int),
+        ("pen_weight", ctypes.c_double),
+        ("pen_div", ctypes.c_double),
+        ("pen_curl", ctypes.c_double),
+        ("pen_norm", ctypes.c_int),
+    ]
+
+
+class MgrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("mgr status %d: %s" % (status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load libmgr.so (raises if it is missing: there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libmgr.so not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != MGR_OK:
+        raise MgrError(status, lib().mgr_last_error().decode())

@@ -1,0 +1,618 @@
+// api.cu — the C ABI of libmgr (include/mgr.h): per-level state, device
+// memory, table upload and the evaluation pipelines.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mgr.h"
+#include "mgr_kernels.hh"
+#include "tables.hh"
+
+namespace mgr {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static thread_local std::string g_err;
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+static void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+        if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
+        throw CudaError(m);
+    }
+}
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        if (count <= n && p) return;
+        release();
+        if (count == 0) return;
+        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        n = count;
+    }
+    void upload(const std::vector<T> &h, cudaStream_t st)
+    {
+        alloc(h.size());
+        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+    }
+};
+
+struct AxisDev {
+    AxisHost h;
+    DevBuf<int> fs, as, rows, ftile0, atile0, gtile;
+    DevBuf<float> fw, aw;
+    void upload(cudaStream_t st)
+    {
+        fs.upload(h.fs, st);
+        as.upload(h.as, st);
+        rows.upload(h.rows, st);
+        ftile0.upload(h.ftile0, st);
+        atile0.upload(h.atile0, st);
+        gtile.upload(h.gtile, st);
+        fw.upload(h.fw, st);
+        aw.upload(h.aw, st);
+    }
+    Axis view() const
+    {
+        Axis a;
+        a.fs = fs.p;
+        a.fw = reinterpret_cast<const float4 *>(fw.p);
+        a.as = as.p;
+        a.aw = reinterpret_cast<const float4 *>(aw.p);
+        a.rows = reinterpret_cast<const int2 *>(rows.p);
+        a.ftile0 = ftile0.p;
+        a.atile0 = atile0.p;
+        a.gtile = reinterpret_cast<const int2 *>(gtile.p);
+        a.n = h.n;
+        a.nc = h.nc;
+        a.t = h.t;
+        a.nt = h.nt;
+        a.fc = h.fc;
+        a.ac = h.ac;
+        return a;
+    }
+};
+
+}  // namespace mgr
+
+using namespace mgr;
+
+struct mgr_level {
+    mgr_level_desc d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int n[3] = {1, 1, 1}, nc[3] = {1, 1, 1};
+    size_t N = 0, ncoef = 0, nparams = 0;
+    int path = MGR_PATH_SPLIT;
+    int tile[3] = {32, 8, 8};
+    AxisDev ax[3];
+    DevBuf<float> coef, ref, warped, minmax, partial, ptable, pen_val;
+    DevBuf<float2> mmpart;
+    DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means;
+    DevBuf<unsigned int> counters;
+    DevBuf<int> pen_rowptr, pen_col;
+    DevBuf<float> grid, force, tmp1, tmp2;   // plain path and standalone force/translate
+    int slot = 0;
+    double center_a = 0.0, center_b = 0.0;
+    bool images_set = false;
+    bool tables_valid = false;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ev_recorded = false;
+    void record(int k)
+    {
+        if (timing) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");
+    }
+    ~mgr_level()
+    {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+
+    EvalArgs args() const
+    {
+        EvalArgs a{};
+        a.dim = d.dim;
+        for (int k = 0; k < 3; ++k) {
+            a.n[k] = n[k];
+            a.nc[k] = nc[k];
+            a.ax[k] = ax[k].view();
+        }
+        a.coef_img = coef.p;
+        a.ref = ref.p;
+        a.warped = warped.p;
+        a.minmax = minmax.p;
+        a.params = params.p;
+        a.cost = d.cost;
+        a.ssd_norm = d.ssd_norm;
+        a.cost_weight = d.cost_weight;
+        a.center_a = center_a;
+        a.center_b = center_b;
+        a.partial = partial.p;
+        a.slot = slot;
+        a.tile_sums = tile_sums.p;
+        a.counters = counters.p;
+        a.scalars = scalars.p;
+        a.has_penalty = d.has_penalty;
+        double prod = double(d.size[0]) * d.size[1] * (d.dim == 3 ? d.size[2] : 1);
+        a.pen_weight = d.pen_norm ? d.pen_weight / double(float(prod)) : d.pen_weight;
+        a.pen_equal_w = d.pen_div == d.pen_curl;
+        a.ptable = ptable.p;
+        a.pen_rowptr = pen_rowptr.p;
+        a.pen_col = pen_col.p;
+        a.pen_val = reinterpret_cast<const float4 *>(pen_val.p);
+        a.pen_part = pen_part.p;
+        a.grad_total = grad_total.p;
+        a.grad_image = nullptr;
+        a.grad_penalty = nullptr;
+        a.costs = costs.p;
+        return a;
+    }
+
+    void build_tables()
+    {
+        const int D = d.dim;
+        for (int k = 0; k < D; ++k) {
+            build_axis(ax[k].h, n[k], nc[k], std::min(tile[k], n[k]));
+            ax[k].upload(stream);
+        }
+        const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
+        slot = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
+        partial.alloc(size_t(ntiles) * slot);
+        const size_t plain_blocks = (N + 255) / 256;
+        tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5);
+        pen_part.alloc((ncoef + 255) / 256 + 1);
+        tables_valid = true;
+    }
+};
+
+static mgr_status fail(mgr_status s, const std::string &m)
+{
+    g_err = m;
+    return s;
+}
+
+template <class F>
+static mgr_status guarded(F f)
+{
+    try {
+        f();
+        return MGR_OK;
+    } catch (const std::invalid_argument &e) {
+        return fail(MGR_ERR_ARG, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(MGR_ERR_OOM, "device or host allocation failed");
+    } catch (const StateError &e) {
+        return fail(MGR_ERR_STATE, e.what());
+    } catch (const CudaError &e) {
+        return fail(MGR_ERR_CUDA, e.what());
+    } catch (const std::exception &e) {
+        return fail(MGR_ERR_CUDA, e.what());
+    }
+}
+
+static void check_launch(const char *what)
+{
+    ck(cudaGetLastError(), what);
+}
+
+extern "C" {
+
+const char *mgr_last_error(void) { return g_err.c_str(); }
+
+unsigned long long mgr_kernel_launch_count(void) { return g_launches.load(); }
+
+mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream, mgr_level **out)
+{
+    if (!desc || !out) return fail(MGR_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<mgr_level> L(new mgr_level);
+    mgr_status st = guarded([&] {
+        const mgr_level_desc &d = *desc;
+        if (d.dim != 2 && d.dim != 3) throw std::invalid_argument("dim must be 2 or 3");
+        if (d.cost != MGR_COST_SSD && d.cost != MGR_COST_NCC) throw std::invalid_argument("unknown cost");
+        if (!std::isfinite(d.cost_weight)) throw std::invalid_argument("cost weight must be finite");
+        if (d.has_penalty && !(std::isfinite(d.pen_weight) && d.pen_weight > 0 && d.pen_div >= 0 && d.pen_curl >= 0))
+            throw std::invalid_argument("penalty weight must be positive, div/curl non-negative");
+        L->d = d;
+        for (int k = 0; k < 3; ++k) {
+            L->n[k] = (k < d.dim) ? d.size[k] : 1;
+            if (k < d.dim) {
+                if (d.size[k] < 2) throw std::invalid_argument("image dimensions must be >= 2");
+                if (d.csize[k] > 0) {
+                    if (d.csize[k] <= 3) throw std::invalid_argument("coefficient grid must be larger than 3 per axis");
+                    L->nc[k] = d.csize[k];
+                } else {
+                    if (!(d.rate[k] >= 1.0f)) throw std::invalid_argument("spline rate must be >= 1");
+                    const int c = csize_from_rate(d.size[k], d.rate[k]);
+                    if (c - 2 <= 1)
+                        throw std::invalid_argument("coefficient rate is too large for the image dimensions");
+                    L->nc[k] = c;
+                }
+            }
+        }
+        L->N = size_t(L->n[0]) * L->n[1] * L->n[2];
+        L->ncoef = size_t(L->nc[0]) * L->nc[1] * L->nc[2];
+        L->nparams = L->ncoef * d.dim;
+        if (d.dim == 2) {
+            L->tile[0] = 32;
+            L->tile[1] = 16;
+            L->tile[2] = 1;
+        }
+        L->device = device;
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        if (stream) {
+            L->stream = static_cast<cudaStream_t>(stream);
+        } else {
+            ck(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            L->own_stream = true;
+        }
+        L->coef.alloc(L->N);
+        L->ref.alloc(L->N);
+        L->warped.alloc(L->N);
+        L->minmax.alloc(2);
+        L->mmpart.alloc(1024);
+        L->params.alloc(L->nparams);
+        L->grad_total.alloc(L->nparams);
+        L->scalars.alloc(SC_NSLOTS);
+        L->costs.alloc(2);
+        L->means.alloc(2);
+        L->counters.alloc(8);
+        ck(cudaMemsetAsync(L->counters.p, 0, 8 * sizeof(unsigned), L->stream), "memset");
+        ck(cudaMemsetAsync(L->scalars.p, 0, SC_NSLOTS * sizeof(double), L->stream), "memset");
+        L->build_tables();
+        if (d.has_penalty) {
+            const float range[3] = {float(d.size[0]), float(d.size[1]), float(d.dim == 3 ? d.size[2] : 1)};
+            if (d.dim == 3) {
+                std::vector<float> P = build_penalty3(L->nc, range, d.pen_div, d.pen_curl);
+                L->ptable.upload(P, L->stream);
+            } else {
+                std::vector<int> rp, col;
+                std::vector<float> val;
+                build_penalty2(L->nc, range, d.pen_div, d.pen_curl, rp, col, val);
+                L->pen_rowptr.upload(rp, L->stream);
+                L->pen_col.upload(col, L->stream);
+                L->pen_val.upload(val, L->stream);
+            }
+        }
+        ck(cudaStreamSynchronize(L->stream), "create sync");
+    });
+    if (st == MGR_OK) *out = L.release();
+    return st;
+}
+
+mgr_status mgr_level_destroy(mgr_level *lvl)
+{
+    if (!lvl) return MGR_OK;
+    cudaSetDevice(lvl->device);
+    if (lvl->stream) cudaStreamSynchronize(lvl->stream);
+    const bool own = lvl->own_stream;
+    cudaStream_t s = lvl->stream;
+    delete lvl;
+    if (own) cudaStreamDestroy(s);
+    return MGR_OK;
+}
+
+mgr_status mgr_level_csize(const mgr_level *lvl, int csize[3], size_t *nparams)
+{
+    if (!lvl) return fail(MGR_ERR_ARG, "null level");
+    if (csize)
+        for (int k = 0; k < 3; ++k) csize[k] = lvl->nc[k];
+    if (nparams) *nparams = lvl->nparams;
+    return MGR_OK;
+}
+
+}  // extern "C"
+
+// mean of a device image in double (NCC provisional centre)
+__global__ void k_mean(const float *__restrict__ img, size_t n, double *out)
+{
+    __shared__ double red[8];
+    double v[1] = {0.0};
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) v[0] += img[i];
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) *out = v[0] / double(n);
+}
+
+static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref)
+{
+    ck(cudaSetDevice(L->device), "cudaSetDevice");
+    cudaStream_t st = L->stream;
+    ck(cudaMemcpyAsync(L->coef.p, d_src, L->N * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy src");
+    if (d_ref != L->ref.p)
+        ck(cudaMemcpyAsync(L->ref.p, d_ref, L->N * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy ref");
+    const int nb = int(std::min<size_t>(1024, (L->N + 255) / 256));
+    launch_minmax(L->coef.p, L->N, L->mmpart.p, nb, L->counters.p + 4, L->minmax.p, st);
+    k_mean<<<1, 256, 0, st>>>(L->coef.p, L->N, L->means.p);
+    k_mean<<<1, 256, 0, st>>>(L->ref.p, L->N, L->means.p + 1);
+    count_launch(2);
+    launch_prefilter(L->coef.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
+    check_launch("set_images kernels");
+    double m[2];
+    ck(cudaMemcpyAsync(m, L->means.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "means");
+    ck(cudaStreamSynchronize(st), "set_images sync");
+    L->center_a = m[0];
+    L->center_b = m[1];
+    L->images_set = true;
+}
+
+static void upload_params(mgr_level *L, const double *params)
+{
+    for (size_t i = 0; i < L->nparams; ++i)
+        if (!std::isfinite(params[i])) throw std::invalid_argument("parameters must be finite");
+    ck(cudaMemcpyAsync(L->params.p, params, L->nparams * sizeof(double), cudaMemcpyHostToDevice, L->stream),
+       "params H2D");
+}
+
+static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
+{
+    cudaStream_t st = L->stream;
+    if (!with_gradient) {
+        launch_warp(a, st);
+        return;
+    }
+    L->ev_recorded = L->timing;
+    if (L->path == MGR_PATH_PLAIN) {
+        L->record(0);
+        const size_t tsz = size_t(std::max(L->nc[2], 1)) * std::max(L->n[1], L->nc[1]) * L->n[0] * 3;
+        if (L->d.dim == 3) L->grid.alloc(L->N * 3);
+        L->force.alloc(L->N * L->d.dim);
+        L->tmp1.alloc(tsz);
+        L->tmp2.alloc(tsz);
+        L->grad_image.alloc(L->nparams);
+        a.grad_image = L->grad_image.p;
+        launch_plain_eval(a, L->grid.p, L->force.p, L->tmp1.p, L->tmp2.p, st);
+        L->record(1);
+        L->record(2);
+        L->record(3);
+        return;
+    }
+    L->record(0);
+    launch_warp(a, st);
+    L->record(1);
+    launch_adjoint(a, st);
+    L->record(2);
+    launch_gather(a, 1, st);
+    L->record(3);
+}
+
+extern "C" {
+
+mgr_status mgr_level_set_images(mgr_level *lvl, const float *src, const float *ref)
+{
+    if (!lvl || !src || !ref) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        for (size_t i = 0; i < lvl->N; ++i)
+            if (!std::isfinite(src[i]) || !std::isfinite(ref[i]))
+                throw std::invalid_argument("images must be finite");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        lvl->warped.alloc(lvl->N);
+        ck(cudaMemcpyAsync(lvl->warped.p, src, lvl->N * sizeof(float), cudaMemcpyHostToDevice, lvl->stream), "src");
+        ck(cudaMemcpyAsync(lvl->ref.p, ref, lvl->N * sizeof(float), cudaMemcpyHostToDevice, lvl->stream), "ref");
+        set_images_impl(lvl, lvl->warped.p, lvl->ref.p);
+    });
+}
+
+mgr_status mgr_level_set_images_device(mgr_level *lvl, const float *d_src, const float *d_ref)
+{
+    if (!lvl || !d_src || !d_ref) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] { set_images_impl(lvl, d_src, d_ref); });
+}
+
+mgr_status mgr_level_evaluate_device(mgr_level *lvl, const double *d_params, double *d_grad_total, double *d_costs)
+{
+    if (!lvl || !d_params || !d_grad_total) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->images_set) throw StateError("set_images must be called before evaluate");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        EvalArgs a = lvl->args();
+        a.params = d_params;
+        a.grad_total = d_grad_total;
+        a.costs = d_costs;
+        run_image_term(lvl, a, true);
+        check_launch("evaluate kernels");
+    });
+}
+
+mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad_total, double *grad_image,
+                              double *grad_penalty, double *cost_image, double *cost_penalty)
+{
+    if (!lvl || !params) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->images_set) throw StateError("set_images must be called before evaluate");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        upload_params(lvl, params);
+        EvalArgs a = lvl->args();
+        if (grad_image && lvl->path != MGR_PATH_PLAIN) {
+            lvl->grad_image.alloc(lvl->nparams);
+            a.grad_image = lvl->grad_image.p;
+        }
+        if (grad_penalty) {
+            lvl->grad_penalty.alloc(lvl->nparams);
+            a.grad_penalty = lvl->grad_penalty.p;
+        }
+        run_image_term(lvl, a, true);
+        check_launch("evaluate kernels");
+        cudaStream_t st = lvl->stream;
+        const size_t bytes = lvl->nparams * sizeof(double);
+        if (grad_total) ck(cudaMemcpyAsync(grad_total, lvl->grad_total.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+        if (grad_image) ck(cudaMemcpyAsync(grad_image, lvl->grad_image.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+        if (grad_penalty)
+            ck(cudaMemcpyAsync(grad_penalty, lvl->grad_penalty.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+        double c[2];
+        ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "evaluate sync");
+        if (cost_image) *cost_image = c[0];
+        if (cost_penalty) *cost_penalty = c[1];
+    });
+}
+
+mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_image, double *cost_penalty)
+{
+    if (!lvl || !params) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->images_set) throw StateError("set_images must be called before value");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        upload_params(lvl, params);
+        EvalArgs a = lvl->args();
+        launch_warp(a, lvl->stream);
+        launch_gather(a, 0, lvl->stream);
+        check_launch("value kernels");
+        double c[2];
+        ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        ck(cudaStreamSynchronize(lvl->stream), "value sync");
+        if (cost_image) *cost_image = c[0];
+        if (cost_penalty) *cost_penalty = c[1];
+    });
+}
+
+mgr_status mgr_level_warp(mgr_level *lvl, const double *params, float *out)
+{
+    if (!lvl || !params || !out) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->images_set) throw StateError("set_images must be called before warp");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        upload_params(lvl, params);
+        EvalArgs a = lvl->args();
+        launch_warp(a, lvl->stream);
+        check_launch("warp kernel");
+        ck(cudaMemcpyAsync(out, lvl->warped.p, lvl->N * sizeof(float), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        ck(cudaStreamSynchronize(lvl->stream), "warp sync");
+    });
+}
+
+mgr_status mgr_level_force(mgr_level *lvl, const double *params, float *force, double *cost)
+{
+    if (!lvl || !params || !force) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->images_set) throw StateError("set_images must be called before force");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        upload_params(lvl, params);
+        EvalArgs a = lvl->args();
+        launch_warp(a, lvl->stream);
+        lvl->force.alloc(lvl->N * lvl->d.dim);
+        launch_force(a, lvl->force.p, lvl->stream);
+        check_launch("force kernels");
+        ck(cudaMemcpyAsync(force, lvl->force.p, lvl->N * lvl->d.dim * sizeof(float), cudaMemcpyDeviceToHost,
+                           lvl->stream), "D2H");
+        double sc[SC_NSLOTS];
+        ck(cudaMemcpyAsync(sc, lvl->scalars.p, sizeof sc, cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        ck(cudaStreamSynchronize(lvl->stream), "force sync");
+        if (cost) *cost = sc[SC_FORCE_COST];
+    });
+}
+
+mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad)
+{
+    if (!lvl || !force || !grad) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        cudaStream_t st = lvl->stream;
+        const int D = lvl->d.dim;
+        lvl->force.alloc(lvl->N * D);
+        const size_t tsz = size_t(std::max(lvl->nc[2], 1)) * std::max(lvl->n[1], lvl->nc[1]) * lvl->n[0] * 3;
+        lvl->tmp1.alloc(tsz);
+        lvl->tmp2.alloc(tsz);
+        lvl->grad_image.alloc(lvl->nparams);
+        ck(cudaMemcpyAsync(lvl->force.p, force, lvl->N * D * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+        EvalArgs a = lvl->args();
+        a.cost_weight = 1.0;
+        launch_translate(a, lvl->force.p, lvl->grad_image.p, lvl->tmp1.p, lvl->tmp2.p, st);
+        check_launch("translate kernels");
+        ck(cudaMemcpyAsync(grad, lvl->grad_image.p, lvl->nparams * sizeof(double), cudaMemcpyDeviceToHost, st),
+           "D2H");
+        ck(cudaStreamSynchronize(st), "translate sync");
+    });
+}
+
+mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z)
+{
+    if (!lvl) return fail(MGR_ERR_ARG, "null level");
+    if (path != MGR_PATH_SPLIT && path != MGR_PATH_PLAIN) return fail(MGR_ERR_ARG, "unknown path");
+    return guarded([&] {
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        lvl->path = path;
+        const int t[3] = {tile_x, tile_y, tile_z};
+        bool changed = false;
+        for (int k = 0; k < lvl->d.dim; ++k)
+            if (t[k] > 0 && t[k] != lvl->tile[k]) {
+                if (k == 0 && t[k] % 32 != 0) throw std::invalid_argument("tile_x must be a multiple of 32");
+                if (t[k] > 128) throw std::invalid_argument("tile length must be <= 128");
+                lvl->tile[k] = t[k];
+                changed = true;
+            }
+        if (changed) {
+            ck(cudaStreamSynchronize(lvl->stream), "sync");
+            lvl->build_tables();
+            ck(cudaStreamSynchronize(lvl->stream), "sync");
+        }
+    });
+}
+
+mgr_status mgr_level_set_timing(mgr_level *lvl, int enable)
+{
+    if (!lvl) return fail(MGR_ERR_ARG, "null level");
+    return guarded([&] {
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        if (enable)
+            for (auto &e : lvl->ev)
+                if (!e) ck(cudaEventCreate(&e), "cudaEventCreate");
+        lvl->timing = enable != 0;
+    });
+}
+
+mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4])
+{
+    if (!lvl || !ms) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (!lvl->ev_recorded) throw StateError("no timed evaluation recorded");
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        ck(cudaEventSynchronize(lvl->ev[3]), "cudaEventSynchronize");
+        float t;
+        for (int k = 0; k < 3; ++k) {
+            ck(cudaEventElapsedTime(&t, lvl->ev[k], lvl->ev[k + 1]), "elapsed");
+            ms[k] = t;
+        }
+        ck(cudaEventElapsedTime(&t, lvl->ev[0], lvl->ev[3]), "elapsed");
+        ms[3] = t;
+    });
+}
+
+mgr_status mgr_level_sync(mgr_level *lvl)
+{
+    if (!lvl) return fail(MGR_ERR_ARG, "null level");
+    return guarded([&] {
+        ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        ck(cudaStreamSynchronize(lvl->stream), "sync");
+    });
+}
+
+}  // extern "C"

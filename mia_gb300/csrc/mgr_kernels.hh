@@ -1,0 +1,68 @@
+// mgr_kernels.hh — host-side launchers of the libmgr kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "mgr_common.cuh"
+
+namespace mgr {
+
+// launch accounting (mgr_kernel_launch_count)
+void count_launch(unsigned n = 1);
+
+void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
+void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
+                   float *out, cudaStream_t st);
+
+// ---- the evaluation pipeline ----------------------------------------
+struct EvalArgs {
+    int dim;
+    int n[3];              // image size
+    int nc[3];             // coefficient grid
+    Axis ax[3];            // per-axis tables (ax[2] unused in 2D)
+    const float *coef_img; // prefiltered moving image
+    const float *ref;      // reference image
+    float *warped;         // warped moving image (N)
+    const float *minmax;   // device {min, max} clamp bounds
+    const double *params;  // spline parameters, interleaved, device
+    int cost;              // MGR_COST_SSD / NCC
+    int ssd_norm;
+    double cost_weight;
+    double center_a, center_b;  // NCC provisional centres (reduce cancellation)
+    // tile partials and reductions
+    float *partial;        // per tile adjoint footprint partials
+    int slot;              // floats per tile slot
+    double *tile_sums;     // per warp tile: 5 doubles
+    unsigned int *counters;// [0] warp, [1] gather, [2] penalty value
+    double *scalars;       // SC_* slots
+    // penalty
+    int has_penalty;
+    double pen_weight;     // effective weight (norm already applied)
+    int pen_equal_w;       // div == curl (multiply skips the cross terms)
+    const float *ptable;   // 3D: 9x9x9 cells x 6 floats (xx, xy, yy, yz, zz, xz)
+    const int *pen_rowptr; // 2D: CSR rows of the boundary-clipped matrix
+    const int *pen_col;
+    const float4 *pen_val; // 2D: (vx, vy, v12, 0)
+    double *pen_part;      // per gather block: penalty value partial
+    // outputs (device)
+    double *grad_total;
+    double *grad_image;    // optional
+    double *grad_penalty;  // optional
+    double *costs;         // optional {cost_image, cost_penalty}
+};
+
+// SPLIT path: warp (+cost sums), gradient/force/adjoint, gather(+penalty)
+void launch_warp(const EvalArgs &a, cudaStream_t st);
+void launch_adjoint(const EvalArgs &a, cudaStream_t st);
+void launch_gather(const EvalArgs &a, int with_gradient, cudaStream_t st);
+int  gather_blocks(const EvalArgs &a);
+
+// standalone pieces for tests and the plain path
+void launch_force(const EvalArgs &a, float *force, cudaStream_t st);       // force field from `warped`
+void launch_translate(const EvalArgs &a, const float *force, double *grad, float *tmp1,
+                      float *tmp2, cudaStream_t st);                         // plain separable adjoint
+void launch_plain_eval(const EvalArgs &a, float *grid, float *force, float *tmp1, float *tmp2,
+                       cudaStream_t st);                                     // PLAIN path image term
+
+}  // namespace mgr

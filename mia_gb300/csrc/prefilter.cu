@@ -1,0 +1,163 @@
+// prefilter.cu — cubic B-spline prefilter (causal/anticausal IIR, pole
+// sqrt(3)-2, mirror boundary) and the image min/max used by the
+// interpolator's clamp.  Restates T3DConvoluteInterpolator::prefilter
+// (mia/3d/interpolator.cxx:98-164) with CSplineBoundaryCondition::filter_line
+// (mia/core/boundary_conditions.cc:62-103) and CMirrorOnBoundary
+// (mia/core/splinebc/bc.cc:67-88): x lines, then y lines, then z lines, each
+// line filtered in double and stored back as float.
+#include "mgr_common.cuh"
+#include "mgr_kernels.hh"
+
+namespace mgr {
+
+// One block of 32 threads owns up to `lb` (<= 32) lines of length n staged
+// in shared memory as double (pitch n+1); each thread filters one line
+// entirely in double, like the reference's double line buffer, and the
+// result is stored back as float.
+// axis 0: lines along x (rows, consecutive rows per block);
+// axis 1/2: lines along y/z (columns of consecutive x per block).
+__global__ void __launch_bounds__(32) k_prefilter_lines(float *__restrict__ img, int nx, int ny, int nz,
+                                                        int axis, int lb)
+{
+    extern __shared__ double sl[];
+    const int t = threadIdx.x;
+    const size_t nxy = size_t(nx) * ny;
+    int n, nl;
+    size_t base, estride;
+    if (axis == 0) {
+        n = nx;
+        const int l0 = blockIdx.x * lb;
+        nl = min(lb, ny * nz - l0);
+        base = size_t(l0) * nx;
+        for (int l = 0; l < nl; ++l)
+            for (int k = t; k < n; k += 32) sl[l * (n + 1) + k] = img[base + size_t(l) * nx + k];
+        estride = 1;
+    } else {
+        const int xb = blockIdx.x * lb;
+        const int other = blockIdx.y;
+        n = (axis == 1) ? ny : nz;
+        base = (axis == 1) ? size_t(other) * nxy + xb : size_t(other) * nx + xb;
+        estride = (axis == 1) ? size_t(nx) : nxy;
+        nl = min(lb, nx - xb);
+        if (t < nl)
+            for (int k = 0; k < n; ++k) sl[t * (n + 1) + k] = img[base + t + k * estride];
+    }
+    __syncthreads();
+    if (t < nl && n >= 2) {
+        double *c = sl + t * (n + 1);
+        const double p = 1.7320508075688772 - 2.0;  // sqrt(3) - 2
+        const double lambda = 2.0 - p - 1.0 / p;
+        for (int k = 0; k < n; ++k) c[k] *= lambda;
+        double zn = p;
+        const double iz = 1.0 / p;
+        double z2n = pow(p, double(n - 1));
+        double sum = c[0] + z2n * c[n - 1];
+        z2n *= z2n * iz;
+        for (int k = 1; k < n - 1; ++k) {
+            sum += (zn + z2n) * c[k];
+            zn *= p;
+            z2n *= iz;
+        }
+        c[0] = sum / (1.0 - zn * zn);
+        for (int k = 1; k < n; ++k) c[k] += p * c[k - 1];
+        c[n - 1] = (p / (p * p - 1.0)) * (p * c[n - 2] + c[n - 1]);
+        for (int k = n - 2; k >= 0; --k) c[k] = p * (c[k + 1] - c[k]);
+    }
+    __syncthreads();
+    if (axis == 0) {
+        for (int l = 0; l < nl; ++l)
+            for (int k = t; k < n; k += 32) img[base + size_t(l) * nx + k] = float(sl[l * (n + 1) + k]);
+    } else if (t < nl) {
+        for (int k = 0; k < n; ++k) img[base + t + k * estride] = float(sl[t * (n + 1) + k]);
+    }
+}
+
+// min/max of the source image with the reference's rule that the lower
+// clamp bound is at most 0 (interpolator.cxx:109-112).  Per-block results
+// go to `part`; the last block to finish reduces them in a fixed order.
+__global__ void __launch_bounds__(256) k_minmax(const float *__restrict__ img, size_t n, float2 *part,
+                                                unsigned int *counter, float *out_minmax)
+{
+    __shared__ float smin[256], smax[256];
+    __shared__ bool last;
+    float mn = INFINITY, mx = -INFINITY;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float v = img[i];
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+    }
+    smin[threadIdx.x] = mn;
+    smax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smin[threadIdx.x] = fminf(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmaxf(smax[threadIdx.x], smax[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = make_float2(smin[0], smax[0]);
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        float a = INFINITY, b = -INFINITY;
+        for (unsigned i = 0; i < gridDim.x; ++i) {
+            const volatile float *v = reinterpret_cast<volatile float *>(part) + 2 * i;
+            a = fminf(a, v[0]);
+            b = fmaxf(b, v[1]);
+        }
+        if (0.0f < a) a = 0.0f;
+        out_minmax[0] = a;
+        out_minmax[1] = b;
+        *counter = 0;
+    }
+}
+
+static int lines_per_block(int n)
+{
+    int lb = 32;
+    while (lb > 1 && size_t(lb) * (n + 1) * sizeof(double) > 160 * 1024) lb >>= 1;
+    return lb;
+}
+
+void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st)
+{
+    if (dim == 2) nz = 1;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_prefilter_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    {
+        const int lb = lines_per_block(nx);
+        const int nlines = ny * nz;
+        const size_t sm = size_t(lb) * (nx + 1) * sizeof(double);
+        k_prefilter_lines<<<(nlines + lb - 1) / lb, 32, sm, st>>>(img, nx, ny, nz, 0, lb);
+        count_launch();
+    }
+    {
+        const int lb = lines_per_block(ny);
+        const size_t sm = size_t(lb) * (ny + 1) * sizeof(double);
+        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, nz), 32, sm, st>>>(img, nx, ny, nz, 1, lb);
+        count_launch();
+    }
+    if (dim == 3 && nz > 1) {
+        const int lb = lines_per_block(nz);
+        const size_t sm = size_t(lb) * (nz + 1) * sizeof(double);
+        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, ny), 32, sm, st>>>(img, nx, ny, nz, 2, lb);
+        count_launch();
+    }
+}
+
+void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
+                   float *out, cudaStream_t st)
+{
+    k_minmax<<<nblocks, 256, 0, st>>>(img, n, part, counter, out);
+    count_launch();
+}
+
+}  // namespace mgr

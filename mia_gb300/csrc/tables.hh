@@ -1,0 +1,27 @@
+// tables.hh — host-side per-level tables (see tables.cc).
+#pragma once
+
+#include <vector>
+
+namespace mgr {
+
+struct AxisHost {
+    int n = 0, nc = 0, t = 0, nt = 0, fc = 0, ac = 0;
+    float scale = 0.0f;
+    std::vector<int> fs;       // n
+    std::vector<float> fw;     // n x 4
+    std::vector<int> as;       // n
+    std::vector<float> aw;     // n x 4
+    std::vector<int> rows;     // nc x (first, len)
+    std::vector<int> ftile0;   // nt
+    std::vector<int> atile0;   // nt
+    std::vector<int> gtile;    // nc x (lo, hi)
+};
+
+int csize_from_rate(int size, float rate);
+void build_axis(AxisHost &ax, int n, int nc, int tile);
+std::vector<float> build_penalty3(const int csize[3], const float range[3], double wdiv, double wrot);
+void build_penalty2(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
+                    std::vector<int> &col, std::vector<float> &val);
+
+}  // namespace mgr

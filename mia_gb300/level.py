@@ -1,0 +1,159 @@
+"""Python front end of one registration level on the GPU.
+
+A ``Level`` owns an ``mgr_level`` of libmgr: the `spline` transformation
+(cubic B-spline coefficients), the `image` full cost with the `ssd` or
+`ncc` image cost and the optional `divcurl` spline penalty, evaluated as
+TNonrigRegGradientProblem::evaluate_fdf does
+(mia/template/nonrigidregister.cxx:415-439).  Arrays are numpy, indexed
+[z, y, x] (x fastest) like MIA's data fields; parameter vectors are MIA's
+interleaved CDoubleVector layout.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Level:
+    """One image pair at one resolution level on one GPU.
+
+    size_xyz      image size (x, y[, z])
+    rate          spline `rate` (scalar or per axis); ignored with `csize`
+    csize         explicit coefficient grid (incl. the 2-coefficient border)
+    cost          'ssd' or 'ncc'
+    ssd_norm      ssd `norm`
+    cost_weight   image full-cost `weight`
+    penalty_weight  divcurl `weight` (None: no penalty); div/curl/penalty_norm
+    """
+
+    def __init__(self, size_xyz, rate=None, csize=None, cost="ssd", ssd_norm=False, cost_weight=1.0,
+                 penalty_weight=None, div=1.0, curl=1.0, penalty_norm=False, device=0, stream=None):
+        d = _lib.LevelDesc()
+        d.dim = len(size_xyz)
+        d.size = (ctypes.c_int * 3)(*(list(size_xyz) + [1] * (3 - d.dim)))
+        d.csize = (ctypes.c_int * 3)(*(list(csize if csize is not None else [0] * d.dim) + [0] * (3 - d.dim)))
+        r = rate if rate is not None else 1.0
+        if not hasattr(r, "__len__"):
+            r = [r] * d.dim
+        d.rate = (ctypes.c_float * 3)(*(list(r) + [1.0] * (3 - len(r))))
+        d.cost = _lib.COST_NCC if cost == "ncc" else _lib.COST_SSD
+        d.ssd_norm = int(ssd_norm)
+        d.cost_weight = float(cost_weight)
+        d.has_penalty = int(penalty_weight is not None)
+        d.pen_weight = float(penalty_weight or 0.0)
+        d.pen_div, d.pen_curl, d.pen_norm = float(div), float(curl), int(penalty_norm)
+        self.desc = d
+        self.dim = d.dim
+        self.size = tuple(size_xyz)
+        h = ctypes.c_void_p()
+        check(lib().mgr_level_create(ctypes.byref(d), int(device), stream, ctypes.byref(h)))
+        self.h = h
+        cs = (ctypes.c_int * 3)()
+        n = ctypes.c_size_t()
+        check(lib().mgr_level_csize(self.h, cs, ctypes.byref(n)))
+        self.csize = tuple(cs[: self.dim])
+        self.nparams = n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mgr_level_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def shape(self):
+        return tuple(self.size[::-1])
+
+    def set_path(self, path="split", tile=(0, 0, 0)):
+        p = _lib.PATH_PLAIN if path == "plain" else _lib.PATH_SPLIT
+        t = list(tile) + [0] * (3 - len(tile))
+        check(lib().mgr_level_set_path(self.h, p, *t))
+
+    def set_images(self, src, ref):
+        s, r = _f(src), _f(ref)
+        assert s.shape == self.shape and r.shape == self.shape
+        check(lib().mgr_level_set_images(self.h, s.ctypes.data_as(_fp), r.ctypes.data_as(_fp)))
+
+    def set_images_device(self, src_ptr, ref_ptr):
+        check(lib().mgr_level_set_images_device(self.h, ctypes.c_void_p(src_ptr), ctypes.c_void_p(ref_ptr)))
+
+    def evaluate(self, params):
+        """(cost_image, cost_penalty, grad_image, grad_penalty, grad_total)"""
+        p = _d(params)
+        assert p.size == self.nparams
+        gt = np.empty(self.nparams)
+        gi = np.empty(self.nparams)
+        gp = np.empty(self.nparams)
+        ci, cp = ctypes.c_double(), ctypes.c_double()
+        check(lib().mgr_level_evaluate(self.h, p.ctypes.data_as(_dp), gt.ctypes.data_as(_dp),
+                                       gi.ctypes.data_as(_dp), gp.ctypes.data_as(_dp), ctypes.byref(ci),
+                                       ctypes.byref(cp)))
+        return ci.value, cp.value, gi, gp, gt
+
+    def evaluate_total(self, params, grad_out=None):
+        """cost+gradient as evaluate_fdf returns it (total cost, total gradient)."""
+        p = _d(params)
+        g = grad_out if grad_out is not None else np.empty(self.nparams)
+        ci, cp = ctypes.c_double(), ctypes.c_double()
+        check(lib().mgr_level_evaluate(self.h, p.ctypes.data_as(_dp), g.ctypes.data_as(_dp), None, None,
+                                       ctypes.byref(ci), ctypes.byref(cp)))
+        return ci.value + cp.value, g
+
+    def evaluate_device(self, params_ptr, grad_ptr, costs_ptr):
+        check(lib().mgr_level_evaluate_device(self.h, ctypes.c_void_p(params_ptr), ctypes.c_void_p(grad_ptr),
+                                              ctypes.c_void_p(costs_ptr)))
+
+    def value(self, params):
+        p = _d(params)
+        ci, cp = ctypes.c_double(), ctypes.c_double()
+        check(lib().mgr_level_value(self.h, p.ctypes.data_as(_dp), ctypes.byref(ci), ctypes.byref(cp)))
+        return ci.value, cp.value
+
+    def warp(self, params):
+        p = _d(params)
+        out = np.empty(self.shape, np.float32)
+        check(lib().mgr_level_warp(self.h, p.ctypes.data_as(_dp), out.ctypes.data_as(_fp)))
+        return out
+
+    def force(self, params):
+        p = _d(params)
+        out = np.empty(self.shape + (self.dim,), np.float32)
+        c = ctypes.c_double()
+        check(lib().mgr_level_force(self.h, p.ctypes.data_as(_dp), out.ctypes.data_as(_fp), ctypes.byref(c)))
+        return c.value, out
+
+    def translate(self, force):
+        f = _f(force)
+        g = np.empty(self.nparams)
+        check(lib().mgr_level_translate(self.h, f.ctypes.data_as(_fp), g.ctypes.data_as(_dp)))
+        return g
+
+    def set_timing(self, enable=True):
+        check(lib().mgr_level_set_timing(self.h, int(enable)))
+
+    def kernel_times(self):
+        """device ms of the last evaluation: (warp, adjoint, gather, total)"""
+        ms = (ctypes.c_double * 4)()
+        check(lib().mgr_level_kernel_times(self.h, ms))
+        return tuple(ms)
+
+    def sync(self):
+        check(lib().mgr_level_sync(self.h))

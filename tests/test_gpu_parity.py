@@ -1,0 +1,244 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances: cost 1e-5 relative, coefficient gradients 1e-4 relative L2
+(against the oracle's reference-precision evaluation); the error against
+the all-double oracle is asserted with the same bounds.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+COST_RTOL = 1e-5
+GRAD_RTOL = 1e-4
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_pair(shape, seed, ncc=False):
+    from mia_gb300 import synth
+    ref = synth.blob_phantom(shape, 10, sigma=(2.0, 5.0), seed=seed)
+    mov = synth.blob_phantom(shape, 10, sigma=(2.0, 5.0), seed=seed)
+    mov = np.roll(mov, 1, axis=-1)
+    if ncc:
+        mov = (mov * synth.bias_field(shape, 0.1, seed=seed + 1)).astype(np.float32)
+    return mov, ref
+
+
+def both(size_xyz, **kw):
+    import mia_gb300 as M
+    g = M.Level(size_xyz, **kw)
+    o = O.Level(size_xyz, precision=O.PREC_REF, **kw)
+    o64 = O.Level(size_xyz, precision=O.PREC_F64, **kw)
+    return g, o, o64
+
+
+def check_eval(g, o, o64, params, path="split", grad_tol=GRAD_RTOL):
+    g.set_path(path)
+    ci, cp, gi, gp, gt = g.evaluate(params)
+    oi, op, ogi, ogp = o.evaluate(params)
+    fi, fp, fgi, fgp = o64.evaluate(params)
+    assert rel(ci, oi) < COST_RTOL, (ci, oi)
+    assert rel(ci, fi) < COST_RTOL, (ci, fi)
+    assert rel_l2(gi, ogi) < grad_tol, rel_l2(gi, ogi)
+    assert rel_l2(gi, fgi) < grad_tol, rel_l2(gi, fgi)
+    if o.desc.has_penalty:
+        assert rel(cp, op) < COST_RTOL, (cp, op)
+        assert rel_l2(gp, ogp) < grad_tol
+        assert rel_l2(gp, fgp) < grad_tol
+    np.testing.assert_array_equal(gt, gi + gp)
+    return ci, cp, gi, gp
+
+
+@pytest.mark.parametrize("cost", ["ssd", "ncc"])
+@pytest.mark.parametrize("path", ["split", "plain"])
+def test_eval_3d(cost, path):
+    size = (37, 29, 21)
+    g, o, o64 = both(size, rate=5.0, cost=cost, penalty_weight=10.0)
+    mov, ref = make_pair(size[::-1], 3, ncc=cost == "ncc")
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 1.5, seed=7)
+    check_eval(g, o, o64, p, path)
+
+
+@pytest.mark.parametrize("cost", ["ssd", "ncc"])
+@pytest.mark.parametrize("path", ["split", "plain"])
+def test_eval_2d(cost, path):
+    size = (61, 47)
+    g, o, o64 = both(size, rate=8.0, cost=cost, penalty_weight=10.0)
+    mov, ref = make_pair(size[::-1], 5, ncc=cost == "ncc")
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 1.5, seed=9)
+    # the 2D image cost is the float-accumulated force-pass cost in the
+    # reference (mia/2d/fullcost/image.cc:100); the GPU sums in double
+    check_eval(g, o, o64, p, path)
+
+
+def test_ssd_norm_and_weight_3d():
+    size = (24, 20, 18)
+    g, o, o64 = both(size, rate=4.0, cost="ssd", ssd_norm=True, cost_weight=0.7, penalty_weight=3.0,
+                     div=0.5, curl=2.0, penalty_norm=True)
+    mov, ref = make_pair(size[::-1], 11)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 2.0, seed=1))
+
+
+def test_value_matches_oracle():
+    size = (33, 27, 19)
+    g, o, _ = both(size, rate=6.0, cost="ncc", penalty_weight=5.0, div=1.0, curl=0.3)
+    mov, ref = make_pair(size[::-1], 13, ncc=True)
+    g.set_images(mov, ref)
+    o.set_images(mov, ref)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 1.0, seed=4)
+    ci, cp = g.value(p)
+    oi, op = o.value(p)
+    assert rel(ci, oi) < COST_RTOL and rel(cp, op) < COST_RTOL
+
+
+def test_warp_and_translate_3d():
+    size = (30, 22, 17)
+    g, o, _ = both(size, rate=4.0)
+    mov, ref = make_pair(size[::-1], 2)
+    g.set_images(mov, ref)
+    o.set_images(mov, ref)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 2.0, seed=5)
+    wg, wo = g.warp(p), o.warp(p)
+    assert np.max(np.abs(wg - wo)) <= 1e-5 * np.max(np.abs(wo))
+    f = np.random.default_rng(0).normal(size=wo.shape + (3,)).astype(np.float32)
+    assert rel_l2(g.translate(f), o.translate(f)) < 1e-5
+    cg, fg = g.force(p)
+    co, fo = o.force(p)
+    assert rel_l2(fg, fo) < 1e-4
+
+
+def test_golden_shift_through_gpu(goldens):
+    import mia_gb300 as M
+    gd = goldens["test_splines_transform"]
+    n = gd["size"]
+    img = np.zeros(n[::-1], np.float32)
+    img[gd["src_slice_z"]] = np.array(gd["src"], np.float32).reshape(10, 10)
+    lv = M.Level(tuple(n), csize=tuple(gd["coeff_size"]))
+    lv.set_images(img, img)
+    w = lv.warp(np.tile(np.array(gd["shift"]), lv.nparams // 3))[gd["ref_slice_z"]]
+    want = np.array(gd["ref"], np.float32).reshape(10, 10)
+    m = (want > gd["compare_if_above"]) | (w > gd["compare_if_above"])
+    np.testing.assert_allclose(w[m], want[m], rtol=gd["tol_pct"] / 100)
+
+
+def test_golden_translate_through_gpu(goldens):
+    import mia_gb300 as M
+    gd = goldens["test_splines_translate"]
+    r = gd["range"]
+    lv = M.Level(tuple(r), csize=tuple(gd["coeff_size"]))
+    force = np.broadcast_to(np.array(gd["force"], np.float32), tuple(r[::-1]) + (3,))
+    gr = lv.translate(force)
+    cs = lv.csize
+    scale = np.prod([(cs[i] - 3) / (r[i] - 1.0) for i in range(3)])
+    gr = gr.reshape(cs[2], cs[1], cs[0], 3) * scale
+    inner = gr[3:cs[2] - 2, 3:cs[1] - 2, 3:cs[0] - 2].reshape(-1, 3)
+    np.testing.assert_allclose(inner, np.broadcast_to(gd["expect_scaled"], inner.shape), rtol=gd["tol_pct"] / 100)
+
+
+def test_golden_ssd_force_through_gpu(goldens):
+    """identity transform: the warped image reproduces the source, so the
+    force equals the reference's SSD golden (mia/3d/cost/test_ssd.cc)."""
+    import mia_gb300 as M
+    gd = goldens["test_SSD_3D"]
+    a = np.array(gd["src"], np.float32).reshape(3, 3, 3)
+    b = np.array(gd["ref"], np.float32).reshape(3, 3, 3)
+    lv = M.Level((3, 3, 3), csize=(4, 4, 4))
+    lv.set_images(a, b)
+    c, f = lv.force(np.zeros(lv.nparams))
+    np.testing.assert_allclose(f[1, 1, 1], gd["force_111"], rtol=1e-5)
+    assert rel(lv.value(np.zeros(lv.nparams))[0], gd["value"]) < gd["value_tol_pct"] / 100
+
+
+@pytest.mark.parametrize("size,rate", [((5, 4, 4), 1.0), ((65, 9, 7), 2.0), ((31, 33, 35), 32.0)])
+def test_edge_sizes(size, rate):
+    g, o, o64 = both(size, rate=rate, cost="ssd", penalty_weight=1.0)
+    mov, ref = make_pair(size[::-1], 17)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 0.8, seed=2))
+
+
+def test_tiles_and_determinism():
+    size = (70, 41, 23)
+    g, o, o64 = both(size, rate=5.0, cost="ncc", penalty_weight=2.0)
+    mov, ref = make_pair(size[::-1], 23, ncc=True)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 1.0, seed=3)
+    ref_out = None
+    for tile in ((32, 8, 8), (64, 4, 4), (32, 16, 2), (96, 8, 8)):
+        g.set_path("split", tile)
+        out = g.evaluate(p)
+        check_eval(g, o, o64, p, "split")
+        if ref_out is None:
+            ref_out = out
+        again = g.evaluate(p)
+        np.testing.assert_array_equal(out[4], again[4])   # bit-identical repeat
+        assert rel_l2(out[4], ref_out[4]) < 1e-5
+
+
+def test_image_gradient_vs_fp64_finite_differences():
+    """The image term's gradient against central differences of the FP64
+    oracle cost (the gradient is the reference's: force from central
+    differences of the warped image, so agreement is to the FD accuracy of
+    a smooth problem, not exact)."""
+    size = (28, 24, 20)
+    g, _, o64 = both(size, rate=5.0, cost="ssd")
+    from mia_gb300 import synth
+    ref = synth.blob_phantom(size[::-1], 6, sigma=(4.0, 7.0), noise=0.0, seed=1)
+    mov = synth.blob_phantom(size[::-1], 6, sigma=(4.0, 7.0), noise=0.0, seed=2)
+    g.set_images(mov, ref)
+    o64.set_images(mov, ref)
+    p = synth.smooth_params(g.csize, 0.5, seed=6)
+    _, _, gi, _, _ = g.evaluate(p)
+    rng = np.random.default_rng(0)
+    idx = rng.choice(np.flatnonzero(np.abs(gi) > 1e-3 * np.abs(gi).max()), 24, replace=False)
+    h = 1e-3
+    fd = []
+    for i in idx:
+        pp = p.copy(); pp[i] += h
+        pm = p.copy(); pm[i] -= h
+        fd.append((o64.value(pp)[0] - o64.value(pm)[0]) / (2 * h))
+    assert rel_l2(gi[idx], np.array(fd)) < 2e-2
+
+
+def test_penalty_gradient_is_minus_fd():
+    """Q1: the penalty's value_and_gradient returns -weight * gradient."""
+    size = (24, 24, 24)
+    g, _, o64 = both(size, rate=4.0, cost="ssd", penalty_weight=10.0)
+    z = np.zeros(size[::-1], np.float32)
+    g.set_images(z, z)
+    o64.set_images(z, z)
+    from mia_gb300 import synth
+    p = synth.smooth_params(g.csize, 1.0, seed=8)
+    _, _, _, gp, _ = g.evaluate(p)
+    rng = np.random.default_rng(1)
+    idx = rng.choice(p.size, 20, replace=False)
+    h = 1e-4
+    for i in idx:
+        pp = p.copy(); pp[i] += h
+        pm = p.copy(); pm[i] -= h
+        fd = (o64.value(pp)[1] - o64.value(pm)[1]) / (2 * h)
+        assert abs(gp[i] + fd) <= 1e-3 * max(1.0, abs(fd))
