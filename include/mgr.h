@@ -139,6 +139,23 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
 mgr_status mgr_level_set_timing(mgr_level *lvl, int enable);
 mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4]);
 
+/* Spline adjoint (translate, 3D) for callers that cannot allocate device
+   memory: code running under CUDA stream capture, hosts that own all device
+   memory through their own arena, latency-bound callers that cannot afford
+   cudaMalloc's implicit synchronisation.  No counterpart in the reference.
+   The caller passes the force field (d_force: size[0]*size[1]*size[2]
+   voxels x 3 floats, device) and receives the negated transposed-spline
+   contraction in d_grad (csize product x 3 doubles, device), identical to
+   mgr_level_translate; it runs asynchronously on `stream` (NULL: the legacy
+   default stream) of the calling thread's current device and allocates
+   nothing.  Intermediates live in one fixed 16 MiB device array per GPU
+   (reserved when the library loads, held until exit); sizes needing more
+   are rejected with MGR_ERR_ARG.  The first call on a device looks up that
+   array's device address, so make it before any stream capture.  Calls
+   share the array: calls whose kernels overlap on the GPU race. */
+mgr_status mgr_translate3d_noalloc(const int size[3], const int csize[3], const float *d_force,
+                                   double *d_grad, void *stream);
+
 /* Wait for all work queued on the level's stream. */
 mgr_status mgr_level_sync(mgr_level *lvl);
 

@@ -37,6 +37,7 @@ SIGNATURES = {
     "mgr_level_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "mgr_level_kernel_times": (ctypes.c_int, [_vp, _dp]),
     "mgr_level_sync": (ctypes.c_int, [_vp]),
+    "mgr_translate3d_noalloc": (ctypes.c_int, [_ip, _ip, _vp, _vp, _vp]),
 }
 
 

@@ -18,6 +18,7 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 static thread_local std::string g_err;
+void set_last_error(const std::string &msg) { g_err = msg; }
 
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
