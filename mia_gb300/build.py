@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libmgr.so")
 BUILD = os.path.join(HERE, "_build")
 
-CU_SOURCES = ["api.cu", "eval.cu", "prefilter.cu", "noalloc.cu"]
+CU_SOURCES = ["api.cu", "eval.cu", "split.cu", "prefilter.cu", "noalloc.cu"]
 CXX_SOURCES = ["tables.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -182,7 +182,7 @@ struct mgr_level {
     {
         const int D = d.dim;
         for (int k = 0; k < D; ++k) {
-            build_axis(ax[k].h, n[k], nc[k], std::min(tile[k], n[k]));
+            build_axis(ax[k].h, n[k], nc[k], tile[k]);
             ax[k].upload(stream);
         }
         const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
@@ -190,7 +190,7 @@ struct mgr_level {
         partial.alloc(size_t(ntiles) * slot);
         const size_t plain_blocks = (N + 255) / 256;
         tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5);
-        pen_part.alloc((ncoef + 255) / 256 + 1);
+        pen_part.alloc(size_t(gather_blocks(args())) + 1);
         tables_valid = true;
     }
 };
@@ -561,12 +561,15 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
     return guarded([&] {
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
         lvl->path = path;
-        const int t[3] = {tile_x, tile_y, tile_z};
+        int t[3] = {tile_x > 0 ? tile_x : lvl->tile[0], tile_y > 0 ? tile_y : lvl->tile[1],
+                    tile_z > 0 ? tile_z : lvl->tile[2]};
+        if (lvl->d.dim == 2) t[2] = 1;
+        if (!tile_supported(lvl->d.dim, t[0], t[1], t[2]))
+            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x8, 32x8x4, 32x4x4, 64x4x4, "
+                                        "64x8x4, 32x16x4, 32x16x8; 2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
         bool changed = false;
-        for (int k = 0; k < lvl->d.dim; ++k)
-            if (t[k] > 0 && t[k] != lvl->tile[k]) {
-                if (k == 0 && t[k] % 32 != 0) throw std::invalid_argument("tile_x must be a multiple of 32");
-                if (t[k] > 128) throw std::invalid_argument("tile length must be <= 128");
+        for (int k = 0; k < 3; ++k)
+            if (t[k] != lvl->tile[k]) {
                 lvl->tile[k] = t[k];
                 changed = true;
             }

@@ -64,15 +64,28 @@ __device__ __forceinline__ float sample3(const float *__restrict__ c, int nx, in
     bspline3_weights(pz - float(fz), wz);
     int ix[4], iy[4], iz[4];
     const int sx = fx - 1, sy = fy - 1, sz = fz - 1;
-    const bool inx = (sx >= 0) && (sx + 3 < nx);
-    const bool iny = (sy >= 0) && (sy + 3 < ny);
-    const bool inz = (sz >= 0) && (sz + 3 < nz);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        ix[k] = inx ? sx + k : mirror_fold(sx + k, nx);
-        iy[k] = (iny ? sy + k : mirror_fold(sy + k, ny)) * nx;
-        iz[k] = (inz ? sz + k : mirror_fold(sz + k, nz));
+        ix[k] = sx + k;
+        iy[k] = sy + k;
+        iz[k] = sz + k;
     }
+    // the mirror fold runs only near the border (a real branch, so the
+    // interior path does not pay for the modulo)
+    if (sx < 0 || sx + 3 >= nx) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ix[k] = mirror_fold(ix[k], nx);
+    }
+    if (sy < 0 || sy + 3 >= ny) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) iy[k] = mirror_fold(iy[k], ny);
+    }
+    if (sz < 0 || sz + 3 >= nz) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) iz[k] = mirror_fold(iz[k], nz);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) iy[k] *= nx;
     const size_t nxy = size_t(nx) * ny;
     float acc = 0.0f;
 #pragma unroll
@@ -101,13 +114,21 @@ __device__ __forceinline__ float sample2(const float *__restrict__ c, int nx, in
     bspline3_weights(py - float(fy), wy);
     int ix[4], iy[4];
     const int sx = fx - 1, sy = fy - 1;
-    const bool inx = (sx >= 0) && (sx + 3 < nx);
-    const bool iny = (sy >= 0) && (sy + 3 < ny);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        ix[k] = inx ? sx + k : mirror_fold(sx + k, nx);
-        iy[k] = (iny ? sy + k : mirror_fold(sy + k, ny)) * nx;
+        ix[k] = sx + k;
+        iy[k] = sy + k;
     }
+    if (sx < 0 || sx + 3 >= nx) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ix[k] = mirror_fold(ix[k], nx);
+    }
+    if (sy < 0 || sy + 3 >= ny) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) iy[k] = mirror_fold(iy[k], ny);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) iy[k] *= nx;
     float acc = 0.0f;
 #pragma unroll
     for (int ky = 0; ky < 4; ++ky) {

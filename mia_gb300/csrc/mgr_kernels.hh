@@ -56,7 +56,11 @@ struct EvalArgs {
 void launch_warp(const EvalArgs &a, cudaStream_t st);
 void launch_adjoint(const EvalArgs &a, cudaStream_t st);
 void launch_gather(const EvalArgs &a, int with_gradient, cudaStream_t st);
+// dense = 1: the image gradient is read from a.grad_image (plain path)
+void launch_gather_mode(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st);
 int  gather_blocks(const EvalArgs &a);
+// tile shapes compiled into the split path
+bool tile_supported(int dim, int tx, int ty, int tz);
 
 // standalone pieces for tests and the plain path
 void launch_force(const EvalArgs &a, float *force, cudaStream_t st);       // force field from `warped`

@@ -1,0 +1,625 @@
+// split.cu — the split evaluation path (default):
+//
+//   k_warp_t<D,TX,TY,TZ>     per voxel tile: the tile's coefficient footprint
+//       is contracted along z, y, x in shared memory (C3DSplineTransformation::
+//       init_grid, mia/3d/transform/spline.cc:541-653) to the displacement
+//       u(x); the prefiltered moving image is sampled with the tricubic
+//       B-spline at x - u(x) (mia/3d/interpolator.cxx:250-287, mirror
+//       boundary, clamp); the warped image is written and the SSD / NCC sums
+//       accumulated; the last block to finish finalises the cost.
+//   k_adjoint_t<D,TX,TY,TZ>  per voxel tile: central differences of the
+//       warped image (mia/3d/image.cc:347-466), the SSD / NCC force
+//       (mia/template/ssd.hh:126-181, mia/3d/cost/ncc.cc:88-128), and the
+//       transposed spline contraction (translate, spline.cc:731-791) of the
+//       force onto the tile's coefficient footprint, x then y then z, each
+//       stage as a sliding 4-coefficient window over monotone start indices;
+//       the result goes to the tile's partial slot (no atomics).
+//   k_gather_w<D>            one warp per coefficient: the fixed-order sum of
+//       the partial slots holding it, the divcurl stencil value and gradient
+//       (mia/3d/ppmatrix.cc:292-599, mia/2d/ppmatrix.cc:245-352), the weighted
+//       and signed total; the last block finalises the costs.
+#include "mgr_cost.cuh"
+
+namespace mgr {
+
+namespace {
+
+constexpr int NT = 256;
+
+struct RowMap {
+    int ix, r0, rstep;
+    bool act;
+};
+
+// rows of runtime width `w`: thread -> (column ix, first row r0), rows
+// advance by rstep; threads beyond rstep*w idle
+__device__ __forceinline__ RowMap row_map(int w)
+{
+    RowMap m;
+    m.ix = threadIdx.x % w;
+    m.r0 = threadIdx.x / w;
+    m.rstep = NT / w;
+    m.act = m.r0 < m.rstep;
+    return m;
+}
+
+// Transposed B-spline contraction of one line of `len` samples onto nout
+// coefficients: sample i contributes w_i[k] * in[i*stride] to coefficient
+// start_i + k (k < 4), start_i non-decreasing.  Four running sums are kept;
+// when the start advances the lowest one is final and emitted.  Every output
+// in [0, nout) is emitted exactly once, in increasing order.
+template <class Emit>
+__device__ __forceinline__ void window_contract(int len, const int *start, const float4 *w, const float *in,
+                                                int stride, int nout, Emit emit)
+{
+    int oc = 0;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    for (int i = 0; i < len; ++i) {
+        const int o = start[i];
+        while (oc < o) {
+            emit(oc, a0);
+            a0 = a1;
+            a1 = a2;
+            a2 = a3;
+            a3 = 0.0f;
+            ++oc;
+        }
+        const float4 ww = w[i];
+        const float f = in[i * stride];
+        a0 += ww.x * f;
+        a1 += ww.y * f;
+        a2 += ww.z * f;
+        a3 += ww.w * f;
+    }
+    if (oc < nout) emit(oc, a0);
+    if (oc + 1 < nout) emit(oc + 1, a1);
+    if (oc + 2 < nout) emit(oc + 2, a2);
+    if (oc + 3 < nout) emit(oc + 3, a3);
+    for (int o = oc + 4; o < nout; ++o) emit(o, 0.0f);
+}
+
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------
+// warp
+// ---------------------------------------------------------------------
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
+{
+    extern __shared__ float sm[];
+    __shared__ double red[5 * (NT / 32)];
+    __shared__ bool is_last;
+    __shared__ int fsx[TX], fsy[TY], fsz[TZ];
+    __shared__ float4 fwx[TX], fwy[TY], fwz[TZ];
+    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
+    const int nx = a.n[0], ny = a.n[1], nz = (D == 3) ? a.n[2] : 1;
+    const int bx = blockIdx.x, by = blockIdx.y, bz = (D == 3) ? blockIdx.z : 0;
+    const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
+    const int ex = min(TX, nx - x0), ey = min(TY, ny - y0), ez = min(TZ, nz - z0);
+    const int FX = X.fc, FY = Y.fc, FZ = (D == 3) ? Z.fc : 1;
+    const int cx0 = X.ftile0[bx], cy0 = Y.ftile0[by], cz0 = (D == 3) ? Z.ftile0[bz] : 0;
+    const int ncx = a.nc[0], ncy = a.nc[1], ncz = (D == 3) ? a.nc[2] : 1;
+    const int tid = threadIdx.x;
+
+    float *C = sm;                                       // [D][FZ][FY][FX]
+    float *T1 = C + D * FZ * FY * FX;                    // [D][TZ][FY][FX]   (3D)
+    float *T2 = T1 + ((D == 3) ? D * TZ * FY * FX : 0);  // [D][TZ][TY][FX]
+
+    // per-tile forward tables (voxels past the image edge repeat the last one)
+    if (tid < TX) {
+        const int x = min(x0 + tid, nx - 1);
+        fsx[tid] = X.fs[x] - cx0;
+        fwx[tid] = X.fw[x];
+    }
+    if (tid < TY) {
+        const int y = min(y0 + tid, ny - 1);
+        fsy[tid] = Y.fs[y] - cy0;
+        fwy[tid] = Y.fw[y];
+    }
+    if (D == 3 && tid < TZ) {
+        const int z = min(z0 + tid, nz - 1);
+        fsz[tid] = Z.fs[z] - cz0;
+        fwz[tid] = Z.fw[z];
+    }
+    const RowMap m = row_map(FX);
+    // coefficient footprint, rows (comp, iz, iy); parameters are double,
+    // interleaved per node
+    if (m.act) {
+        const int gx = cx0 + m.ix;
+        for (int r = m.r0; r < D * FZ * FY; r += m.rstep) {
+            const int comp = r / (FZ * FY), rr = r - comp * FZ * FY;
+            const int iz = rr / FY, iy = rr - iz * FY;
+            const int gy = cy0 + iy, gz = cz0 + iz;
+            float v = 0.0f;
+            if (gx < ncx && gy < ncy && gz < ncz)
+                v = float(a.params[((size_t(gz) * ncy + gy) * ncx + gx) * D + comp]);
+            C[r * FX + m.ix] = v;
+        }
+    }
+    __syncthreads();
+    if (D == 3) {
+        if (m.act) {
+            const int st = FY * FX;
+            for (int r = m.r0; r < D * TZ * FY; r += m.rstep) {
+                const int comp = r / (TZ * FY), rr = r - comp * TZ * FY;
+                const int zz = rr / FY, iy = rr - zz * FY;
+                const int s = fsz[zz];
+                const float4 w = fwz[zz];
+                const float *c = C + (comp * FZ * FY + iy) * FX + m.ix + s * st;
+                T1[r * FX + m.ix] = w.x * c[0] + w.y * c[st] + w.z * c[2 * st] + w.w * c[3 * st];
+            }
+        }
+        __syncthreads();
+    }
+    {
+        const float *Src = (D == 3) ? T1 : C;  // [D][TZ][FY][FX] (2D: TZ = FZ = 1)
+        if (m.act) {
+            for (int r = m.r0; r < D * TZ * TY; r += m.rstep) {
+                const int comp = r / (TZ * TY), rr = r - comp * (TZ * TY);
+                const int zz = rr / TY, yy = rr - zz * TY;
+                const int s = fsy[yy];
+                const float4 w = fwy[yy];
+                const float *c = Src + ((comp * TZ + zz) * FY + s) * FX + m.ix;
+                T2[r * FX + m.ix] = w.x * c[0] + w.y * c[FX] + w.z * c[2 * FX] + w.w * c[3 * FX];
+            }
+        }
+    }
+    __syncthreads();
+
+    // x stage, tricubic sample, warped image, sums
+    float acc[5] = {0, 0, 0, 0, 0};
+    const float mn = a.minmax[0], mxv = a.minmax[1];
+    const float ca = float(a.center_a), cb = float(a.center_b);
+    constexpr int NV = TX * TY * TZ;
+    for (int v = tid; v < NV; v += NT) {
+        const int xx = v % TX, yy = (v / TX) % TY, zz = v / (TX * TY);
+        if (xx >= ex || yy >= ey || zz >= ez) continue;
+        const int x = x0 + xx, y = y0 + yy, z = z0 + zz;
+        const int s = fsx[xx];
+        const float4 w = fwx[xx];
+        float u[3];
+#pragma unroll
+        for (int comp = 0; comp < D; ++comp) {
+            const float *c = T2 + ((comp * TZ + zz) * TY + yy) * FX + s;
+            u[comp] = w.x * c[0] + w.y * c[1] + w.z * c[2] + w.w * c[3];
+        }
+        float wv;
+        if (D == 3)
+            wv = sample3(a.coef_img, nx, ny, nz, float(x) - u[0], float(y) - u[1], float(z) - u[2], mn, mxv);
+        else
+            wv = sample2(a.coef_img, nx, ny, float(x) - u[0], float(y) - u[1], mn, mxv);
+        const size_t idx = (size_t(z) * ny + y) * nx + x;
+        a.warped[idx] = wv;
+        const float b = a.ref[idx];
+        if (a.cost == 0) {
+            const float d = wv - b;
+            acc[0] += d * d;
+        } else {
+            const float da = wv - ca, db = b - cb;
+            acc[0] += da;
+            acc[1] += db;
+            acc[2] += da * da;
+            acc[3] += db * db;
+            acc[4] += da * db;
+        }
+    }
+    double dv[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dv[k] = acc[k];
+    block_sum<5>(dv, red);
+    const int ntiles = gridDim.x * gridDim.y * gridDim.z;
+    const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) a.tile_sums[size_t(tile) * 5 + k] = dv[k];
+        __threadfence();
+        is_last = (atomicAdd(&a.counters[0], 1u) == unsigned(ntiles - 1));
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        reduce_tile_sums(a, ntiles, size_t(nx) * ny * nz, red);
+        if (tid == 0) a.counters[0] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------
+// gradient + force + adjoint
+// ---------------------------------------------------------------------
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
+{
+    extern __shared__ float sm[];
+    constexpr int HX = TX + 2, HY = TY + 2, HZ = (D == 3) ? TZ + 2 : 1;
+    constexpr int TXP = TX + 1;
+    __shared__ int asx[TX], asy[TY], asz[TZ];
+    __shared__ float4 awx[TX], awy[TY], awz[TZ];
+    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
+    const int nx = a.n[0], ny = a.n[1], nz = (D == 3) ? a.n[2] : 1;
+    const int bx = blockIdx.x, by = blockIdx.y, bz = (D == 3) ? blockIdx.z : 0;
+    const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
+    const int ex = min(TX, nx - x0), ey = min(TY, ny - y0), ez = min(TZ, nz - z0);
+    const int AXc = X.ac, AYc = Y.ac, AZc = (D == 3) ? Z.ac : 1;
+    const int ax0 = X.atile0[bx], ay0 = Y.atile0[by], az0 = (D == 3) ? Z.atile0[bz] : 0;
+    const int tid = threadIdx.x;
+    const size_t tile = (size_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    float *part = a.partial + tile * a.slot;
+
+    float *Wh = sm;                          // [HZ][HY][HX]
+    float *F = Wh + HZ * HY * HX;            // [D][TZ][TY][TXP]
+    float *AX = F + D * TZ * TY * TXP;       // [D][TZ][TY][AXc]
+    float *AY = AX + D * TZ * TY * AXc;      // [D][TZ][AYc][AXc]   (3D)
+
+    if (tid < TX) {
+        const int x = min(x0 + tid, nx - 1);
+        asx[tid] = X.as[x] - ax0;
+        awx[tid] = X.aw[x];
+    }
+    if (tid < TY) {
+        const int y = min(y0 + tid, ny - 1);
+        asy[tid] = Y.as[y] - ay0;
+        awy[tid] = Y.aw[y];
+    }
+    if (D == 3 && tid < TZ) {
+        const int z = min(z0 + tid, nz - 1);
+        asz[tid] = Z.as[z] - az0;
+        awz[tid] = Z.aw[z];
+    }
+    // warped image with a one-voxel halo, zero outside the image
+    for (int e = tid; e < HZ * HY * HX; e += NT) {
+        const int hx = e % HX, hy = (e / HX) % HY, hz = e / (HX * HY);
+        const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = (D == 3) ? z0 - 1 + hz : 0;
+        float v = 0.0f;
+        if (x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz) v = a.warped[(size_t(z) * ny + y) * nx + x];
+        Wh[e] = v;
+    }
+    __syncthreads();
+    {
+        const double *sc = a.scalars;
+        const float k1 = float(sc[SC_K1]), k2 = float(sc[SC_K2]);
+        const float ma = float(sc[SC_MA]), mb = float(sc[SC_MB]), fscale = float(sc[SC_FSCALE]);
+        constexpr int NV = TX * TY * TZ;
+        for (int v = tid; v < NV; v += NT) {
+            const int xx = v % TX, yy = (v / TX) % TY, zz = v / (TX * TY);
+            float f[3] = {0.0f, 0.0f, 0.0f};
+            if (xx < ex && yy < ey && zz < ez) {
+                const int x = x0 + xx, y = y0 + yy, z = z0 + zz;
+                const int c = (((D == 3) ? zz + 1 : 0) * HY + yy + 1) * HX + xx + 1;
+                const float w = Wh[c];
+                float g[3];
+                g[0] = (x > 0 && x < nx - 1) ? 0.5f * (Wh[c + 1] - Wh[c - 1]) : 0.0f;
+                g[1] = (y > 0 && y < ny - 1) ? 0.5f * (Wh[c + HX] - Wh[c - HX]) : 0.0f;
+                if (D == 3) g[2] = (z > 0 && z < nz - 1) ? 0.5f * (Wh[c + HX * HY] - Wh[c - HX * HY]) : 0.0f;
+                const float b = a.ref[(size_t(z) * ny + y) * nx + x];
+                if (a.cost == 0) {
+                    const float d = w - b;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) f[k] = (g[k] * d) * fscale;
+                } else {
+                    const float s = k1 * (k2 * (w - ma) - (b - mb));
+#pragma unroll
+                    for (int k = 0; k < D; ++k) f[k] = s * g[k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < D; ++k) F[((k * TZ + zz) * TY + yy) * TXP + xx] = f[k];
+        }
+    }
+    __syncthreads();
+    // x: rows (comp, zz, yy)
+    for (int r = tid; r < D * TZ * TY; r += NT) {
+        float *out = AX + r * AXc;
+        window_contract(ex, asx, awx, F + r * TXP, 1, AXc, [&](int o, float v) { out[o] = v; });
+    }
+    __syncthreads();
+    // y: columns (comp*TZ + zz, ox)
+    for (int c = tid; c < D * TZ * AXc; c += NT) {
+        const int ox = c % AXc, cz = c / AXc;
+        const float *in = AX + cz * TY * AXc + ox;
+        if (D == 3) {
+            float *out = AY + cz * AYc * AXc + ox;
+            window_contract(ey, asy, awy, in, AXc, AYc, [&](int o, float v) { out[o * AXc] = v; });
+        } else {
+            const int comp = cz;
+            window_contract(ey, asy, awy, in, AXc, AYc,
+                            [&](int o, float v) { part[(size_t(o) * AXc + ox) * D + comp] = v; });
+        }
+    }
+    if (D == 3) {
+        __syncthreads();
+        // z: columns (oy, ox, comp), comp fastest so the slot writes coalesce
+        for (int c = tid; c < D * AYc * AXc; c += NT) {
+            const int comp = c % D, rest = c / D;
+            const int ox = rest % AXc, oy = rest / AXc;
+            const float *in = AY + (comp * TZ * AYc + oy) * AXc + ox;
+            window_contract(ez, asz, awz, in, AYc * AXc, AZc, [&](int o, float v) {
+                part[((size_t(o) * AYc + oy) * AXc + ox) * D + comp] = v;
+            });
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// gather + divcurl penalty + costs, one warp per coefficient
+// ---------------------------------------------------------------------
+// 3D penalty table: cell (dx,dy,dz) at ((dz*9 + dy)*9 + dx)*6 holding
+// (xx, xy, yy, yz, zz, xz), index = i - j + 4 per axis.
+template <int D>
+__global__ void __launch_bounds__(NT) k_gather_w(EvalArgs a, int with_gradient, int image_from_dense)
+{
+    extern __shared__ float sm[];
+    __shared__ double red[NT / 32];
+    __shared__ float wval[NT / 32];
+    __shared__ bool is_last;
+    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
+    const int ncx = a.nc[0], ncy = a.nc[1], ncz = (D == 3) ? a.nc[2] : 1;
+    const size_t ncoef = size_t(ncx) * ncy * ncz;
+    const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+    if (D == 3 && a.has_penalty) {
+        for (int e = tid; e < 9 * 9 * 9 * 6; e += NT) sm[e] = a.ptable[e];
+        __syncthreads();
+    }
+    const size_t i = (size_t(blockIdx.x) * NT + tid) >> 5;
+    float pval = 0.0f;
+    if (i < ncoef) {
+        const int cx = int(i % ncx), cy = int((i / ncx) % ncy), cz = (D == 3) ? int(i / (size_t(ncx) * ncy)) : 0;
+        double gimg[3] = {0.0, 0.0, 0.0};
+        if (with_gradient) {
+            if (image_from_dense) {
+#pragma unroll
+                for (int k = 0; k < D; ++k) gimg[k] = a.grad_image[i * D + k];
+            } else {
+                const int2 gx = X.gtile[cx], gy = Y.gtile[cy];
+                const int2 gz = (D == 3) ? Z.gtile[cz] : make_int2(0, 0);
+                const int nX = gx.y - gx.x + 1, nY = gy.y - gy.x + 1, nZ = gz.y - gz.x + 1;
+                const int total = (nX > 0 && nY > 0 && nZ > 0) ? nX * nY * nZ : 0;
+                float s[3] = {0.0f, 0.0f, 0.0f};
+                for (int k = lane; k < total; k += 32) {
+                    const int tx = gx.x + k % nX, ty = gy.x + (k / nX) % nY, tz = gz.x + k / (nX * nY);
+                    const int lx = cx - X.atile0[tx], ly = cy - Y.atile0[ty];
+                    const int lz = (D == 3) ? cz - Z.atile0[tz] : 0;
+                    const size_t t = (size_t(tz) * Y.nt + ty) * X.nt + tx;
+                    const float *p = a.partial + t * a.slot + ((size_t(lz) * Y.ac + ly) * X.ac + lx) * D;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) s[c] += p[c];
+                }
+#pragma unroll
+                for (int c = 0; c < D; ++c) gimg[c] = a.cost_weight * (-double(warp_sum_f(s[c])));
+            }
+        }
+        double gpen[3] = {0.0, 0.0, 0.0};
+        if (a.has_penalty) {
+            float g[3] = {0.0f, 0.0f, 0.0f};
+            float r[6] = {0, 0, 0, 0, 0, 0};
+            if (D == 3) {
+                const int zl = max(0, cz - 4), zh = min(cz + 4, ncz);
+                const int yl = max(0, cy - 4), yh = min(cy + 4, ncy);
+                const int xl = max(0, cx - 4), xh = min(cx + 4, ncx);
+                const int ny_ = yh - yl, pairs = (zh - zl) * ny_;
+                for (int p = lane; p < pairs; p += 32) {
+                    const int zj = zl + p / ny_, yj = yl + p % ny_;
+                    const int dz = cz - zj + 4, dy = cy - yj + 4;
+                    const double *pj = a.params + ((size_t(zj) * ncy + yj) * ncx) * 3;
+                    for (int xj = xl; xj < xh; ++xj) {
+                        const float *P = sm + ((dz * 9 + dy) * 9 + (cx - xj + 4)) * 6;
+                        const float cjx = float(pj[xj * 3]), cjy = float(pj[xj * 3 + 1]), cjz = float(pj[xj * 3 + 2]);
+                        const float vxx = P[0], vxy = P[1], vyy = P[2], vyz = P[3], vzz = P[4], vxz = P[5];
+                        if (with_gradient) {
+                            const float ax = vxx * cjx, az = vxz * cjx;
+                            const float bxy = vxy * cjy, byy = vyy * cjy;
+                            const float cyz = vyz * cjz, czz = vzz * cjz;
+                            r[0] += ax; r[1] += bxy; r[2] += byy; r[3] += cyz; r[4] += czz; r[5] += az;
+                            g[0] += cjz * vxz + (2.0f * ax + bxy);
+                            g[1] += cjx * vxy + (2.0f * byy + cyz);
+                            g[2] += cjy * vyz + (2.0f * czz + az);
+                        } else {
+                            // operator*: ci.x cj.y vxy, ci.x cj.z vxz, ci.y cj.z vyz
+                            r[0] += cjx * vxx; r[2] += cjy * vyy; r[4] += cjz * vzz;
+                            r[1] += cjy * vxy; r[5] += cjz * vxz; r[3] += cjz * vyz;
+                        }
+                    }
+                }
+            } else {
+                for (int e = a.pen_rowptr[i] + lane; e < a.pen_rowptr[i + 1]; e += 32) {
+                    const int j = a.pen_col[e];
+                    const float4 v = a.pen_val[e];
+                    const float cjx = float(a.params[size_t(j) * 2]), cjy = float(a.params[size_t(j) * 2 + 1]);
+                    const float aa = cjx * v.x, bb = cjy * v.y, cxx = cjx * v.z, cyy = cjy * v.z;
+                    g[0] += aa + aa + cyy;
+                    g[1] += bb + bb + cxx;
+                    r[0] += aa;
+                    r[1] += cyy;
+                    r[2] += bb;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) g[k] = warp_sum_f(g[k]);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) r[k] = warp_sum_f(r[k]);
+            float ci[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int k = 0; k < D; ++k) ci[k] = float(a.params[i * D + k]);
+            if (D == 3) {
+                if (with_gradient)
+                    pval = ci[0] * r[0] + ci[0] * r[1] + ci[1] * r[2] + ci[1] * r[3] + ci[2] * r[4] + ci[2] * r[5];
+                else
+                    pval = ci[0] * r[0] + ci[1] * r[2] + ci[2] * r[4] + ci[0] * r[1] + ci[0] * r[5] + ci[1] * r[3];
+            } else {
+                pval = ci[0] * r[0] + ci[0] * r[1] + ci[1] * r[2];
+            }
+#pragma unroll
+            for (int k = 0; k < D; ++k) gpen[k] = -a.pen_weight * double(g[k]);
+        }
+        if (with_gradient && lane < D) {
+            const int k = lane;
+            // select without dynamic register indexing
+            const double gi = (k == 0) ? gimg[0] : (k == 1) ? gimg[1] : gimg[2];
+            const double gp = (k == 0) ? gpen[0] : (k == 1) ? gpen[1] : gpen[2];
+            a.grad_total[i * D + k] = gi + gp;
+            if (a.grad_image && !image_from_dense) a.grad_image[i * D + k] = gi;
+            if (a.grad_penalty) a.grad_penalty[i * D + k] = gp;
+        }
+    }
+    if (lane == 0) wval[wib] = pval;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NT / 32; ++w) s += wval[w];
+        a.pen_part[blockIdx.x] = s;
+        __threadfence();
+        is_last = (atomicAdd(&a.counters[1], 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        double s[1] = {0.0};
+        for (unsigned b = tid; b < gridDim.x; b += NT) s[0] += ((volatile double *)a.pen_part)[b];
+        block_sum<1>(s, red);
+        if (tid == 0) {
+            double *sc = a.scalars;
+            const double pen = a.has_penalty ? s[0] : 0.0;
+            sc[SC_PEN] = pen;
+            const double img = (D == 2 && with_gradient) ? sc[SC_FORCE_COST] : sc[SC_VALUE];
+            sc[SC_COST_IMG] = a.cost_weight * img;
+            sc[SC_COST_PEN] = a.has_penalty ? a.pen_weight * pen : 0.0;
+            if (a.costs) {
+                a.costs[0] = sc[SC_COST_IMG];
+                a.costs[1] = sc[SC_COST_PEN];
+            }
+            a.counters[1] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------
+static size_t warp_smem(const EvalArgs &a)
+{
+    const int D = a.dim;
+    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
+    const int TZ = (D == 3) ? Z.t : 1, FZ = (D == 3) ? Z.fc : 1;
+    size_t f = size_t(D) * FZ * Y.fc * X.fc;
+    if (D == 3) f += size_t(D) * TZ * Y.fc * X.fc;
+    f += size_t(D) * TZ * Y.t * X.fc;
+    return f * sizeof(float);
+}
+
+static size_t adjoint_smem(const EvalArgs &a)
+{
+    const int D = a.dim;
+    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
+    const int TZ = (D == 3) ? Z.t : 1, HZ = (D == 3) ? Z.t + 2 : 1;
+    size_t f = size_t(HZ) * (Y.t + 2) * (X.t + 2);
+    f += size_t(D) * TZ * Y.t * (X.t + 1);
+    f += size_t(D) * TZ * Y.t * X.ac;
+    if (D == 3) f += size_t(D) * TZ * Y.ac * X.ac;
+    return f * sizeof(float);
+}
+
+static dim3 tile_grid(const EvalArgs &a)
+{
+    return dim3(a.ax[0].nt, a.ax[1].nt, a.dim == 3 ? a.ax[2].nt : 1);
+}
+
+template <int D, int TX, int TY, int TZ>
+static void launch_tile(const EvalArgs &a, int which, cudaStream_t st)
+{
+    if (which == 0) {
+        const size_t sm = warp_smem(a);
+        cudaFuncSetAttribute(k_warp_t<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        k_warp_t<D, TX, TY, TZ><<<tile_grid(a), NT, sm, st>>>(a);
+    } else {
+        const size_t sm = adjoint_smem(a);
+        cudaFuncSetAttribute(k_adjoint_t<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        k_adjoint_t<D, TX, TY, TZ><<<tile_grid(a), NT, sm, st>>>(a);
+    }
+    count_launch();
+}
+
+// the tile shapes compiled in (tile_supported() must match)
+static bool dispatch(const EvalArgs &a, int which, cudaStream_t st)
+{
+    const int tx = a.ax[0].t, ty = a.ax[1].t, tz = a.dim == 3 ? a.ax[2].t : 1;
+#define MGR_TILE3(X_, Y_, Z_)                              \
+    if (a.dim == 3 && tx == X_ && ty == Y_ && tz == Z_) {  \
+        launch_tile<3, X_, Y_, Z_>(a, which, st);          \
+        return true;                                       \
+    }
+#define MGR_TILE2(X_, Y_)                                  \
+    if (a.dim == 2 && tx == X_ && ty == Y_) {              \
+        launch_tile<2, X_, Y_, 1>(a, which, st);           \
+        return true;                                       \
+    }
+    MGR_TILE3(32, 8, 8)
+    MGR_TILE3(32, 8, 4)
+    MGR_TILE3(32, 4, 4)
+    MGR_TILE3(64, 4, 4)
+    MGR_TILE3(64, 8, 4)
+    MGR_TILE3(32, 16, 4)
+    MGR_TILE3(32, 16, 8)
+    MGR_TILE2(32, 8)
+    MGR_TILE2(32, 16)
+    MGR_TILE2(64, 8)
+    MGR_TILE2(64, 16)
+    MGR_TILE2(32, 32)
+#undef MGR_TILE3
+#undef MGR_TILE2
+    return false;
+}
+
+bool tile_supported(int dim, int tx, int ty, int tz)
+{
+    static const int t3[][3] = {{32, 8, 8}, {32, 8, 4}, {32, 4, 4}, {64, 4, 4}, {64, 8, 4}, {32, 16, 4}, {32, 16, 8}};
+    static const int t2[][2] = {{32, 8}, {32, 16}, {64, 8}, {64, 16}, {32, 32}};
+    if (dim == 3) {
+        for (auto &t : t3)
+            if (t[0] == tx && t[1] == ty && t[2] == tz) return true;
+    } else {
+        for (auto &t : t2)
+            if (t[0] == tx && t[1] == ty) return true;
+    }
+    return false;
+}
+
+void launch_warp(const EvalArgs &a, cudaStream_t st)
+{
+    dispatch(a, 0, st);
+}
+
+void launch_adjoint(const EvalArgs &a, cudaStream_t st)
+{
+    dispatch(a, 1, st);
+}
+
+int gather_blocks(const EvalArgs &a)
+{
+    const size_t ncoef = size_t(a.nc[0]) * a.nc[1] * (a.dim == 3 ? a.nc[2] : 1);
+    return int((ncoef + NT / 32 - 1) / (NT / 32));
+}
+
+void launch_gather_mode(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st)
+{
+    const int nb = gather_blocks(a);
+    if (a.dim == 3) {
+        const size_t sm = (a.has_penalty ? 9 * 9 * 9 * 6 : 0) * sizeof(float);
+        k_gather_w<3><<<nb, NT, sm, st>>>(a, with_gradient, dense);
+    } else {
+        k_gather_w<2><<<nb, NT, 0, st>>>(a, with_gradient, dense);
+    }
+    count_launch();
+}
+
+void launch_gather(const EvalArgs &a, int with_gradient, cudaStream_t st)
+{
+    launch_gather_mode(a, with_gradient, 0, st);
+}
+
+}  // namespace mgr

@@ -167,7 +167,9 @@ void build_axis(AxisHost &ax, int n, int nc, int tile)
         ax.fc = std::max(ax.fc, ax.fs[v1] + 3 - ax.fs[v0] + 1);
         ax.atile0[b] = ax.as[v0];
         aend[b] = std::min(nc - 1, ax.as[v1] + 3);
-        ax.ac = std::max(ax.ac, aend[b] - ax.atile0[b] + 1);
+        // the slot holds the full 4-wide window of the last voxel, even where
+        // it reaches past the grid (those entries are zero and never read)
+        ax.ac = std::max(ax.ac, ax.as[v1] + 3 - ax.atile0[b] + 1);
         if (ax.fs[v0] < 0) throw std::runtime_error("negative forward start index");
     }
     ax.gtile.assign(size_t(nc) * 2, 0);
