@@ -156,6 +156,58 @@ mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4]);
 mgr_status mgr_translate3d_noalloc(const int size[3], const int csize[3], const float *d_force,
                                    double *d_grad, void *stream);
 
+/* ---- registration driver ------------------------------------------- */
+
+enum { MGR_MIN_GSL_SD = 0, MGR_MIN_GDSQ = 1 };
+
+/* Minimizer parameters, named as the plugin parameters:
+   gsl:opt=gd  -> kind MGR_MIN_GSL_SD, iter=maxiter, step, tol, eps
+                  (defaults 100, 0.001, 0.1, 0.01; mia/core/minimizer/gsl.cc:252-273)
+   gdsq        -> kind MGR_MIN_GDSQ, maxiter, step, scale, xtola=xtol,
+                  gtola=gtol, ftolr, min_step (defaults 100, 0.1, 2, 0, 0, 0,
+                  1e-6; mia/core/minimizer/gdsq.cc:127-147) */
+typedef struct {
+    int    kind;
+    int    maxiter;
+    double step;
+    double tol;
+    double eps;
+    double scale;
+    double xtol, gtol, ftolr, min_step;
+} mgr_minimizer_desc;
+
+/* Replaces: TNonrigidRegisterImpl::run (mia/template/nonrigidregister.cxx:
+   193-296) for the spline transformation with the image (+ divcurl) cost:
+   joint mean-0/sigma-1 normalisation of the pair, `levels` resolution
+   levels (size / 2^shift; the `scale` filter builds each level), upscale of
+   the transformation between levels, the minimizer on every level and again
+   after a refine() that grows the coefficient grid.  `desc` describes the
+   full-size problem (desc->csize must be 0: the grid follows `rate`).
+   `path` selects the evaluation kernels (MGR_PATH_*); the minimizer runs on
+   the host and evaluates through mgr_level_evaluate (one device round trip
+   per evaluation: the plain per-pair drop-in).  Writes the final
+   coefficient grid, its parameters (max_params doubles), the cost at the
+   returned parameters and the number of cost+gradient evaluations. */
+mgr_status mgr_register(const mgr_level_desc *desc, int levels, const mgr_minimizer_desc *mz,
+                        const float *src, const float *ref, int path, int device,
+                        double *params_out, size_t max_params, int csize_out[3],
+                        double *final_cost, int *evaluations);
+
+/* Replaces: the `scale` filter that builds a multiresolution level
+   (C3DScale::operator(), mia/3d/filter/scale.cc:95-118; C2DScale,
+   mia/2d/filter/scale.cc:50-90); downscaling only.  Host images, run on
+   `device`. */
+mgr_status mgr_scale_image(int dim, const int in_size[3], const float *in, const int out_size[3],
+                           float *out, int device);
+
+/* Replaces: FScaleFilterCreator + the linear convert filter it builds
+   (mia/template/nonrigidregister.cxx:147-184): the joint mean-0/sigma-1
+   normalisation of a pair.  Writes the normalised images (host), the mean
+   and sigma; *applied = 0 when both images hold one value (then nothing is
+   written to the outputs). */
+mgr_status mgr_normalize_pair(const float *src, const float *ref, size_t n, float *src_out,
+                              float *ref_out, double *mean, double *sigma, int *applied, int device);
+
 /* Wait for all work queued on the level's stream. */
 mgr_status mgr_level_sync(mgr_level *lvl);
 

@@ -38,6 +38,10 @@ SIGNATURES = {
     "mgr_level_kernel_times": (ctypes.c_int, [_vp, _dp]),
     "mgr_level_sync": (ctypes.c_int, [_vp]),
     "mgr_translate3d_noalloc": (ctypes.c_int, [_ip, _ip, _vp, _vp, _vp]),
+    "mgr_register": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _fp, _fp, ctypes.c_int, ctypes.c_int, _dp,
+                                    ctypes.c_size_t, _ip, _dp, _ip]),
+    "mgr_scale_image": (ctypes.c_int, [ctypes.c_int, _ip, _fp, _ip, _fp, ctypes.c_int]),
+    "mgr_normalize_pair": (ctypes.c_int, [_fp, _fp, ctypes.c_size_t, _fp, _fp, _dp, _dp, _ip, ctypes.c_int]),
 }
 
 
@@ -57,6 +61,37 @@ class LevelDesc(ctypes.Structure):
         ("pen_curl", ctypes.c_double),
         ("pen_norm", ctypes.c_int),
     ]
+
+
+MIN_GSL_SD, MIN_GDSQ = 0, 1
+
+
+class MinimizerDesc(ctypes.Structure):
+    """mgr_minimizer_desc"""
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("maxiter", ctypes.c_int),
+        ("step", ctypes.c_double),
+        ("tol", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("scale", ctypes.c_double),
+        ("xtol", ctypes.c_double),
+        ("gtol", ctypes.c_double),
+        ("ftolr", ctypes.c_double),
+        ("min_step", ctypes.c_double),
+    ]
+
+
+def minimizer(kind="gsl", maxiter=100, step=None, tol=0.1, eps=0.01, scale=2.0, xtol=0.0, gtol=0.0,
+              ftolr=0.0, min_step=1e-6):
+    """gsl:opt=gd (defaults as the plugin, step 0.1 as the CLI) or gdsq"""
+    m = MinimizerDesc()
+    m.kind = MIN_GDSQ if kind == "gdsq" else MIN_GSL_SD
+    m.maxiter = int(maxiter)
+    m.step = float(step if step is not None else 0.1)
+    m.tol, m.eps, m.scale = float(tol), float(eps), float(scale)
+    m.xtol, m.gtol, m.ftolr, m.min_step = float(xtol), float(gtol), float(ftolr), float(min_step)
+    return m
 
 
 class MgrError(RuntimeError):

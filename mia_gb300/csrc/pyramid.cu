@@ -1,0 +1,303 @@
+// pyramid.cu — image preparation of the registration driver on the GPU:
+//
+// * joint intensity normalisation of the pair (FScaleFilterCreator,
+//   mia/template/nonrigidregister.cxx:147-184): sums over both images in
+//   double, then y = float(a*x + b) with a = 1/sigma, b = -mean/sigma, where
+//   a and b pass through the reference's 6-significant-digit filter string;
+// * the `scale` filter that builds each multiresolution level
+//   (C3DScale / C2DScale, mia/3d/filter/scale.cc:95-155,
+//   mia/2d/filter/scale.cc:50-90; C1DScalar::downscale,
+//   mia/core/scaler1d.cc): per axis and per line, in double, a binomial
+//   "gauss:w=round(1/scale)" smoothing with half-sample symmetric borders
+//   (mia/core/spacialkernel/gauss.cc), the mirror-boundary cubic prefilter,
+//   and cubic B-spline resampling at i*(n_in-1)/(n_out-1).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mgr_common.cuh"
+#include "mgr_kernels.hh"
+#include "pyramid.hh"
+
+namespace mgr {
+
+struct Wt4 {
+    double x, y, z, w;
+};
+
+__global__ void k_pair_sums(const float *__restrict__ a, const float *__restrict__ b, size_t n, double *part)
+{
+    __shared__ double red[2 * 8];
+    double v[2] = {0.0, 0.0};
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const double fa = a[i], fb = b[i];
+        v[0] += fa + fb;
+        v[1] += fa * fa + fb * fb;
+    }
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = v[0];
+        part[2 * blockIdx.x + 1] = v[1];
+    }
+}
+
+__global__ void k_apply_linear(const float *__restrict__ in, float *__restrict__ out, size_t n, double a, double b)
+{
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        out[i] = float(fma(a, double(in[i]), b));
+}
+
+// one thread per line; the line and its smoothed copy are staged in shared
+// memory as double (lb lines per block, pitch n_in)
+template <class TI, class TO>
+__global__ void __launch_bounds__(32) k_scale_lines(const TI *__restrict__ in, TO *__restrict__ out, int lb,
+                                                    int n_in, int n_out, int nlines, size_t in_line_stride,
+                                                    size_t in_elem_stride, size_t out_line_stride,
+                                                    size_t out_elem_stride, int lines_per_plane,
+                                                    size_t in_plane_stride, size_t out_plane_stride, int gw,
+                                                    const double *gmask, const int4 *idx, const Wt4 *wts)
+{
+    extern __shared__ double sl[];
+    const int t = threadIdx.x;
+    const int l = blockIdx.x * lb + t;
+    if (t >= lb || l >= nlines) return;
+    double *c = sl + size_t(t) * 2 * n_in;
+    double *s = c + n_in;
+    const int pl = l / lines_per_plane, lp = l % lines_per_plane;
+    const TI *src = in + size_t(pl) * in_plane_stride + size_t(lp) * in_line_stride;
+    TO *dst = out + size_t(pl) * out_plane_stride + size_t(lp) * out_line_stride;
+    for (int k = 0; k < n_in; ++k) c[k] = double(src[k * in_elem_stride]);
+    // binomial smoothing, half-sample symmetric borders
+    if (gw < 0) {  // C1DScalar copies when the size does not change
+        for (int i = 0; i < n_out; ++i) dst[i * out_elem_stride] = TO(c[i]);
+        return;
+    }
+    const int m = 2 * gw + 1;
+    for (int i = 0; i < n_in; ++i) {
+        double h = 0.0;
+        for (int j = 0; j < m; ++j) {
+            int k = i - gw + j;
+            if (k < 0) k = -k - 1;
+            if (k >= n_in) k = 2 * n_in - 1 - k;
+            h += gmask[j] * c[k];
+        }
+        s[i] = h;
+    }
+    // mirror-boundary prefilter (filter_line), in double
+    if (n_in >= 2) {
+        const double p = 1.7320508075688772 - 2.0;
+        const double lambda = 2.0 - p - 1.0 / p;
+        for (int k = 0; k < n_in; ++k) s[k] *= lambda;
+        double zn = p;
+        const double iz = 1.0 / p;
+        double z2n = pow(p, double(n_in - 1));
+        double sum = s[0] + z2n * s[n_in - 1];
+        z2n *= z2n * iz;
+        for (int k = 1; k < n_in - 1; ++k) {
+            sum += (zn + z2n) * s[k];
+            zn *= p;
+            z2n *= iz;
+        }
+        s[0] = sum / (1.0 - zn * zn);
+        for (int k = 1; k < n_in; ++k) s[k] += p * s[k - 1];
+        s[n_in - 1] = (p / (p * p - 1.0)) * (p * s[n_in - 2] + s[n_in - 1]);
+        for (int k = n_in - 2; k >= 0; --k) s[k] = p * (s[k + 1] - s[k]);
+    }
+    for (int i = 0; i < n_out; ++i) {
+        const int4 ix = idx[i];
+        const Wt4 w = wts[i];
+        const double v = w.x * s[ix.x] + w.y * s[ix.y] + w.z * s[ix.z] + w.w * s[ix.w];
+        dst[i * out_elem_stride] = TO(v);
+    }
+}
+
+namespace {
+
+int fastfloor_h(double v)
+{
+    volatile double t = v + 68719476736.0 * 1.5;
+    double tt = t;
+    uint64_t bits;
+    memcpy(&bits, &tt, sizeof bits);
+    return int32_t(uint32_t(bits & 0xffffffffu)) >> 16;
+}
+
+int mirror_h(int index, int width)
+{
+    const int w2 = 2 * width - 2;
+    int idx = index < 0 ? -index : index;
+    idx = (width == 1) ? 0 : ((idx < w2) ? idx : idx % w2);
+    if (width <= idx) idx = w2 - idx;
+    return idx;
+}
+
+void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// per-axis resampling plan of C1DScalar (downscale): gauss half width and
+// the 4 taps + weights of every output sample
+struct AxisPlan {
+    int gw = 0;
+    std::vector<double> mask;
+    std::vector<int4> idx;
+    std::vector<Wt4> wts;
+};
+
+AxisPlan plan_axis(int n_in, int n_out)
+{
+    AxisPlan p;
+    if (n_in == n_out) {
+        p.gw = -1;
+        p.mask.assign(1, 1.0);
+        p.idx.assign(1, make_int4(0, 0, 0, 0));
+        p.wts.assign(1, Wt4{1, 0, 0, 0});
+        return p;
+    }
+    const double scale = double(n_out - 1) / double(n_in - 1);
+    p.gw = int(std::floor(1.0 / scale + 0.5));
+    const int m = 2 * p.gw + 1;
+    std::vector<double> k(m, 0.0);
+    k[0] = 1.0;
+    if (m > 1) k[1] = 1.0;
+    std::vector<double> tmp(m, 0.0);
+    for (int i = 2; i < m; ++i) {
+        k[i] = 1.0;
+        for (int j = 1; j < i; ++j) tmp[j] = k[j - 1] + k[j];
+        for (int j = 1; j < i; ++j) k[j] = tmp[j];
+    }
+    const double norm = std::pow(2.0, m - 1);
+    for (auto &v : k) v /= norm;
+    p.mask = k;
+    const double dx = 1.0 / scale;
+    for (int i = 0; i < n_out; ++i) {
+        const double x = double(i) * dx;
+        const int ix = fastfloor_h(x);
+        const double f = x - ix;
+        const double ob6 = 1.0 / 6.0, xm1 = 1 - f;
+        const double w0 = (xm1 * xm1) * (xm1 * ob6), w3 = (f * f) * (f * ob6);
+        const double w1 = ((xm1 - w0) - w0) + w3, w2 = ((f - w3) - w3) + w0;
+        int id[4];
+        for (int q = 0; q < 4; ++q) id[q] = ix - 1 + q;
+        if (id[0] < 0 || id[3] >= n_in)
+            for (int q = 0; q < 4; ++q) id[q] = mirror_h(id[q], n_in);
+        p.idx.push_back(make_int4(id[0], id[1], id[2], id[3]));
+        p.wts.push_back(Wt4{w0, w1, w2, w3});
+    }
+    return p;
+}
+
+template <class TI, class TO>
+void scale_axis(const TI *in, TO *out, const AxisPlan &p, int n_in, int n_out, int nlines, size_t ils, size_t ies,
+                size_t ols, size_t oes, int lpp, size_t ips, size_t ops, cudaStream_t st)
+{
+    double *d_mask = nullptr;
+    int4 *d_idx = nullptr;
+    Wt4 *d_wts = nullptr;
+    ck(cudaMalloc(&d_mask, p.mask.size() * sizeof(double)), "cudaMalloc");
+    ck(cudaMalloc(&d_idx, p.idx.size() * sizeof(int4)), "cudaMalloc");
+    ck(cudaMalloc(&d_wts, p.wts.size() * sizeof(Wt4)), "cudaMalloc");
+    ck(cudaMemcpyAsync(d_mask, p.mask.data(), p.mask.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(d_idx, p.idx.data(), p.idx.size() * sizeof(int4), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(d_wts, p.wts.data(), p.wts.size() * sizeof(Wt4), cudaMemcpyHostToDevice, st), "H2D");
+    int lb = 32;
+    while (lb > 1 && size_t(lb) * 2 * n_in * sizeof(double) > 160 * 1024) lb >>= 1;
+    const size_t sm = size_t(lb) * 2 * n_in * sizeof(double);
+    cudaFuncSetAttribute(k_scale_lines<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_scale_lines<TI, TO><<<(nlines + lb - 1) / lb, 32, sm, st>>>(in, out, lb, n_in, n_out, nlines, ils, ies, ols, oes,
+                                                                  lpp, ips, ops, p.gw, d_mask, d_idx, d_wts);
+    count_launch();
+    ck(cudaGetLastError(), "scale kernel");
+    ck(cudaStreamSynchronize(st), "scale sync");
+    cudaFree(d_mask);
+    cudaFree(d_idx);
+    cudaFree(d_wts);
+}
+
+}  // namespace
+
+std::string format_g6(double v)
+{
+    char buf[64];
+    snprintf(buf, sizeof buf, "%g", v);
+    return buf;
+}
+
+bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_src_out, float *d_ref_out,
+                    cudaStream_t st, double *mean_out, double *sigma_out)
+{
+    const int nb = int(std::min<size_t>(512, (n + 255) / 256));
+    double *d_part = nullptr;
+    ck(cudaMalloc(&d_part, size_t(nb) * 2 * sizeof(double)), "cudaMalloc");
+    k_pair_sums<<<nb, 256, 0, st>>>(d_src, d_ref, n, d_part);
+    count_launch();
+    std::vector<double> part(size_t(nb) * 2);
+    ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "sync");
+    cudaFree(d_part);
+    double sum = 0.0, sum2 = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        sum += part[2 * b];
+        sum2 += part[2 * b + 1];
+    }
+    const double nn = 2.0 * double(n);
+    const double mean = sum / nn;
+    const double sigma = std::sqrt((sum2 - sum * sum / nn) / (nn - 1));
+    if (mean_out) *mean_out = mean;
+    if (sigma_out) *sigma_out = sigma;
+    if (sigma == 0.0) return false;
+    // the reference passes a and b through "convert:...,b=<v>,a=<v>" with
+    // the default stream precision (6 significant digits)
+    const double b = std::stod(format_g6(-mean / sigma));
+    const double a = std::stod(format_g6(1.0 / sigma));
+    const int nb2 = int(std::min<size_t>(4096, (n + 255) / 256));
+    k_apply_linear<<<nb2, 256, 0, st>>>(d_src, d_src_out, n, a, b);
+    k_apply_linear<<<nb2, 256, 0, st>>>(d_ref, d_ref_out, n, a, b);
+    count_launch(2);
+    ck(cudaGetLastError(), "normalize kernels");
+    return true;
+}
+
+void scale_image(const float *d_in, const int in_size[3], float *d_out, const int out_size[3], int dim,
+                 cudaStream_t st)
+{
+    const int nx = in_size[0], ny = in_size[1], nz = dim == 3 ? in_size[2] : 1;
+    const int mx = out_size[0], my = out_size[1], mz = dim == 3 ? out_size[2] : 1;
+    if (nx == mx && ny == my && nz == mz) {
+        ck(cudaMemcpyAsync(d_out, d_in, size_t(nx) * ny * nz * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+        return;
+    }
+    for (int k = 0; k < dim; ++k)
+        if (out_size[k] > in_size[k] || out_size[k] < 2)
+            throw std::invalid_argument("scale: only downscaling to sizes >= 2 is supported");
+    // x: float -> double, lines = rows (y, z)
+    double *t1 = nullptr, *t2 = nullptr;
+    ck(cudaMalloc(&t1, size_t(mx) * ny * nz * sizeof(double)), "cudaMalloc");
+    const AxisPlan px = plan_axis(nx, mx);
+    const AxisPlan py = plan_axis(ny, my);
+    // C1DScalar copies when the size does not change on an axis
+    auto run_x = [&](auto *out) {
+        scale_axis(d_in, out, px, nx, mx, ny * nz, size_t(nx), 1, size_t(mx), 1, ny * nz, 0, 0, st);
+    };
+    run_x(t1);
+    if (dim == 2) {
+        // y: double -> float, lines = columns x, stride mx
+        scale_axis(t1, d_out, py, ny, my, mx, 1, size_t(mx), 1, size_t(mx), mx, 0, 0, st);
+        cudaFree(t1);
+        return;
+    }
+    ck(cudaMalloc(&t2, size_t(mx) * my * nz * sizeof(double)), "cudaMalloc");
+    // y: lines = (x, z): per plane z, mx lines of stride 1, element stride mx
+    scale_axis(t1, t2, py, ny, my, mx * nz, 1, size_t(mx), 1, size_t(mx), mx, size_t(mx) * ny, size_t(mx) * my, st);
+    // z: lines = (x, y): mx*my lines, element stride mx*my
+    const AxisPlan pz = plan_axis(nz, mz);
+    scale_axis(t2, d_out, pz, nz, mz, mx * my, 1, size_t(mx) * my, 1, size_t(mx) * my, mx * my, 0, 0, st);
+    cudaFree(t1);
+    cudaFree(t2);
+}
+
+}  // namespace mgr

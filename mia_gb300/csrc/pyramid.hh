@@ -1,0 +1,23 @@
+// pyramid.hh — multiresolution image preparation (see pyramid.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <string>
+
+namespace mgr {
+
+// %g formatting (6 significant digits), as a C++ stream writes a double
+std::string format_g6(double v);
+
+// Joint mean-0 / sigma-1 normalisation of a pair; returns false (and writes
+// nothing) when both images hold a single value.
+bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_src_out, float *d_ref_out,
+                    cudaStream_t st, double *mean_out, double *sigma_out);
+
+// The `scale` filter (downscaling only); a copy when the sizes agree.
+void scale_image(const float *d_in, const int in_size[3], float *d_out, const int out_size[3], int dim,
+                 cudaStream_t st);
+
+}  // namespace mgr

@@ -14,10 +14,8 @@
 //       force onto the tile's coefficient footprint, x then y then z, each
 //       stage as a sliding 4-coefficient window over monotone start indices;
 //       the result goes to the tile's partial slot (no atomics).
-//   k_gather_w<D>            one warp per coefficient: the fixed-order sum of
-//       the partial slots holding it, the divcurl stencil value and gradient
-//       (mia/3d/ppmatrix.cc:292-599, mia/2d/ppmatrix.cc:245-352), the weighted
-//       and signed total; the last block finalises the costs.
+// The per-coefficient gather of the partial slots and the divcurl penalty
+// follow in gather.cu.
 #include "mgr_cost.cuh"
 
 namespace mgr {
@@ -76,13 +74,6 @@ __device__ __forceinline__ void window_contract(int len, const int *start, const
     if (oc + 2 < nout) emit(oc + 2, a2);
     if (oc + 3 < nout) emit(oc + 3, a3);
     for (int o = oc + 4; o < nout; ++o) emit(o, 0.0f);
-}
-
-__device__ __forceinline__ float warp_sum_f(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
 }
 
 }  // namespace
@@ -347,158 +338,6 @@ __global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
 }
 
 // ---------------------------------------------------------------------
-// gather + divcurl penalty + costs, one warp per coefficient
-// ---------------------------------------------------------------------
-// 3D penalty table: cell (dx,dy,dz) at ((dz*9 + dy)*9 + dx)*6 holding
-// (xx, xy, yy, yz, zz, xz), index = i - j + 4 per axis.
-template <int D>
-__global__ void __launch_bounds__(NT) k_gather_w(EvalArgs a, int with_gradient, int image_from_dense)
-{
-    extern __shared__ float sm[];
-    __shared__ double red[NT / 32];
-    __shared__ float wval[NT / 32];
-    __shared__ bool is_last;
-    const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
-    const int ncx = a.nc[0], ncy = a.nc[1], ncz = (D == 3) ? a.nc[2] : 1;
-    const size_t ncoef = size_t(ncx) * ncy * ncz;
-    const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-    if (D == 3 && a.has_penalty) {
-        for (int e = tid; e < 9 * 9 * 9 * 6; e += NT) sm[e] = a.ptable[e];
-        __syncthreads();
-    }
-    const size_t i = (size_t(blockIdx.x) * NT + tid) >> 5;
-    float pval = 0.0f;
-    if (i < ncoef) {
-        const int cx = int(i % ncx), cy = int((i / ncx) % ncy), cz = (D == 3) ? int(i / (size_t(ncx) * ncy)) : 0;
-        double gimg[3] = {0.0, 0.0, 0.0};
-        if (with_gradient) {
-            if (image_from_dense) {
-#pragma unroll
-                for (int k = 0; k < D; ++k) gimg[k] = a.grad_image[i * D + k];
-            } else {
-                const int2 gx = X.gtile[cx], gy = Y.gtile[cy];
-                const int2 gz = (D == 3) ? Z.gtile[cz] : make_int2(0, 0);
-                const int nX = gx.y - gx.x + 1, nY = gy.y - gy.x + 1, nZ = gz.y - gz.x + 1;
-                const int total = (nX > 0 && nY > 0 && nZ > 0) ? nX * nY * nZ : 0;
-                float s[3] = {0.0f, 0.0f, 0.0f};
-                for (int k = lane; k < total; k += 32) {
-                    const int tx = gx.x + k % nX, ty = gy.x + (k / nX) % nY, tz = gz.x + k / (nX * nY);
-                    const int lx = cx - X.atile0[tx], ly = cy - Y.atile0[ty];
-                    const int lz = (D == 3) ? cz - Z.atile0[tz] : 0;
-                    const size_t t = (size_t(tz) * Y.nt + ty) * X.nt + tx;
-                    const float *p = a.partial + t * a.slot + ((size_t(lz) * Y.ac + ly) * X.ac + lx) * D;
-#pragma unroll
-                    for (int c = 0; c < D; ++c) s[c] += p[c];
-                }
-#pragma unroll
-                for (int c = 0; c < D; ++c) gimg[c] = a.cost_weight * (-double(warp_sum_f(s[c])));
-            }
-        }
-        double gpen[3] = {0.0, 0.0, 0.0};
-        if (a.has_penalty) {
-            float g[3] = {0.0f, 0.0f, 0.0f};
-            float r[6] = {0, 0, 0, 0, 0, 0};
-            if (D == 3) {
-                const int zl = max(0, cz - 4), zh = min(cz + 4, ncz);
-                const int yl = max(0, cy - 4), yh = min(cy + 4, ncy);
-                const int xl = max(0, cx - 4), xh = min(cx + 4, ncx);
-                const int ny_ = yh - yl, pairs = (zh - zl) * ny_;
-                for (int p = lane; p < pairs; p += 32) {
-                    const int zj = zl + p / ny_, yj = yl + p % ny_;
-                    const int dz = cz - zj + 4, dy = cy - yj + 4;
-                    const double *pj = a.params + ((size_t(zj) * ncy + yj) * ncx) * 3;
-                    for (int xj = xl; xj < xh; ++xj) {
-                        const float *P = sm + ((dz * 9 + dy) * 9 + (cx - xj + 4)) * 6;
-                        const float cjx = float(pj[xj * 3]), cjy = float(pj[xj * 3 + 1]), cjz = float(pj[xj * 3 + 2]);
-                        const float vxx = P[0], vxy = P[1], vyy = P[2], vyz = P[3], vzz = P[4], vxz = P[5];
-                        if (with_gradient) {
-                            const float ax = vxx * cjx, az = vxz * cjx;
-                            const float bxy = vxy * cjy, byy = vyy * cjy;
-                            const float cyz = vyz * cjz, czz = vzz * cjz;
-                            r[0] += ax; r[1] += bxy; r[2] += byy; r[3] += cyz; r[4] += czz; r[5] += az;
-                            g[0] += cjz * vxz + (2.0f * ax + bxy);
-                            g[1] += cjx * vxy + (2.0f * byy + cyz);
-                            g[2] += cjy * vyz + (2.0f * czz + az);
-                        } else {
-                            // operator*: ci.x cj.y vxy, ci.x cj.z vxz, ci.y cj.z vyz
-                            r[0] += cjx * vxx; r[2] += cjy * vyy; r[4] += cjz * vzz;
-                            r[1] += cjy * vxy; r[5] += cjz * vxz; r[3] += cjz * vyz;
-                        }
-                    }
-                }
-            } else {
-                for (int e = a.pen_rowptr[i] + lane; e < a.pen_rowptr[i + 1]; e += 32) {
-                    const int j = a.pen_col[e];
-                    const float4 v = a.pen_val[e];
-                    const float cjx = float(a.params[size_t(j) * 2]), cjy = float(a.params[size_t(j) * 2 + 1]);
-                    const float aa = cjx * v.x, bb = cjy * v.y, cxx = cjx * v.z, cyy = cjy * v.z;
-                    g[0] += aa + aa + cyy;
-                    g[1] += bb + bb + cxx;
-                    r[0] += aa;
-                    r[1] += cyy;
-                    r[2] += bb;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) g[k] = warp_sum_f(g[k]);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) r[k] = warp_sum_f(r[k]);
-            float ci[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-            for (int k = 0; k < D; ++k) ci[k] = float(a.params[i * D + k]);
-            if (D == 3) {
-                if (with_gradient)
-                    pval = ci[0] * r[0] + ci[0] * r[1] + ci[1] * r[2] + ci[1] * r[3] + ci[2] * r[4] + ci[2] * r[5];
-                else
-                    pval = ci[0] * r[0] + ci[1] * r[2] + ci[2] * r[4] + ci[0] * r[1] + ci[0] * r[5] + ci[1] * r[3];
-            } else {
-                pval = ci[0] * r[0] + ci[0] * r[1] + ci[1] * r[2];
-            }
-#pragma unroll
-            for (int k = 0; k < D; ++k) gpen[k] = -a.pen_weight * double(g[k]);
-        }
-        if (with_gradient && lane < D) {
-            const int k = lane;
-            // select without dynamic register indexing
-            const double gi = (k == 0) ? gimg[0] : (k == 1) ? gimg[1] : gimg[2];
-            const double gp = (k == 0) ? gpen[0] : (k == 1) ? gpen[1] : gpen[2];
-            a.grad_total[i * D + k] = gi + gp;
-            if (a.grad_image && !image_from_dense) a.grad_image[i * D + k] = gi;
-            if (a.grad_penalty) a.grad_penalty[i * D + k] = gp;
-        }
-    }
-    if (lane == 0) wval[wib] = pval;
-    __syncthreads();
-    if (tid == 0) {
-        double s = 0.0;
-        for (int w = 0; w < NT / 32; ++w) s += wval[w];
-        a.pen_part[blockIdx.x] = s;
-        __threadfence();
-        is_last = (atomicAdd(&a.counters[1], 1u) == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (is_last) {
-        __threadfence();
-        double s[1] = {0.0};
-        for (unsigned b = tid; b < gridDim.x; b += NT) s[0] += ((volatile double *)a.pen_part)[b];
-        block_sum<1>(s, red);
-        if (tid == 0) {
-            double *sc = a.scalars;
-            const double pen = a.has_penalty ? s[0] : 0.0;
-            sc[SC_PEN] = pen;
-            const double img = (D == 2 && with_gradient) ? sc[SC_FORCE_COST] : sc[SC_VALUE];
-            sc[SC_COST_IMG] = a.cost_weight * img;
-            sc[SC_COST_PEN] = a.has_penalty ? a.pen_weight * pen : 0.0;
-            if (a.costs) {
-                a.costs[0] = sc[SC_COST_IMG];
-                a.costs[1] = sc[SC_COST_PEN];
-            }
-            a.counters[1] = 0;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------
 static size_t warp_smem(const EvalArgs &a)
@@ -597,29 +436,6 @@ void launch_warp(const EvalArgs &a, cudaStream_t st)
 void launch_adjoint(const EvalArgs &a, cudaStream_t st)
 {
     dispatch(a, 1, st);
-}
-
-int gather_blocks(const EvalArgs &a)
-{
-    const size_t ncoef = size_t(a.nc[0]) * a.nc[1] * (a.dim == 3 ? a.nc[2] : 1);
-    return int((ncoef + NT / 32 - 1) / (NT / 32));
-}
-
-void launch_gather_mode(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st)
-{
-    const int nb = gather_blocks(a);
-    if (a.dim == 3) {
-        const size_t sm = (a.has_penalty ? 9 * 9 * 9 * 6 : 0) * sizeof(float);
-        k_gather_w<3><<<nb, NT, sm, st>>>(a, with_gradient, dense);
-    } else {
-        k_gather_w<2><<<nb, NT, 0, st>>>(a, with_gradient, dense);
-    }
-    count_launch();
-}
-
-void launch_gather(const EvalArgs &a, int with_gradient, cudaStream_t st)
-{
-    launch_gather_mode(a, with_gradient, 0, st);
 }
 
 }  // namespace mgr

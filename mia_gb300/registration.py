@@ -1,0 +1,71 @@
+"""Multiresolution registration of image pairs on the GPU.
+
+``register_pair`` follows TNonrigidRegisterImpl::run
+(mia/template/nonrigidregister.cxx:193-296): joint normalisation, levels
+built with the `scale` filter, upscale and refine of the spline
+transformation, the `gsl:opt=gd` or `gdsq` minimizer per level.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib, minimizer  # noqa: F401
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+def level_desc(size_xyz, rate, cost="ssd", penalty_weight=None, div=1.0, curl=1.0, ssd_norm=False,
+               cost_weight=1.0, penalty_norm=False):
+    d = _lib.LevelDesc()
+    d.dim = len(size_xyz)
+    d.size = (ctypes.c_int * 3)(*(list(size_xyz) + [1] * (3 - d.dim)))
+    d.csize = (ctypes.c_int * 3)(0, 0, 0)
+    r = rate if hasattr(rate, "__len__") else [rate] * d.dim
+    d.rate = (ctypes.c_float * 3)(*(list(r) + [1.0] * (3 - len(r))))
+    d.cost = _lib.COST_NCC if cost == "ncc" else _lib.COST_SSD
+    d.ssd_norm, d.cost_weight = int(ssd_norm), float(cost_weight)
+    d.has_penalty = int(penalty_weight is not None)
+    d.pen_weight = float(penalty_weight or 0.0)
+    d.pen_div, d.pen_curl, d.pen_norm = float(div), float(curl), int(penalty_norm)
+    return d
+
+
+def register_pair(src, ref, rate, levels, mz, path="split", device=0, **cost_kw):
+    """Returns (params, csize, final_cost, evaluations)."""
+    s = np.ascontiguousarray(src, dtype=np.float32)
+    r = np.ascontiguousarray(ref, dtype=np.float32)
+    d = level_desc(s.shape[::-1], rate, **cost_kw)
+    maxp = 1 << 24
+    out = np.empty(maxp)
+    cs = (ctypes.c_int * 3)()
+    fc, ne = ctypes.c_double(), ctypes.c_int()
+    p = _lib.PATH_PLAIN if path == "plain" else _lib.PATH_SPLIT
+    check(lib().mgr_register(ctypes.byref(d), int(levels), ctypes.byref(mz), s.ctypes.data_as(_fp),
+                             r.ctypes.data_as(_fp), p, int(device), out.ctypes.data_as(_dp), maxp, cs,
+                             ctypes.byref(fc), ctypes.byref(ne)))
+    dim = d.dim
+    n = int(np.prod(cs[:dim])) * dim
+    return out[:n].copy(), tuple(cs[:dim]), fc.value, ne.value
+
+
+def scale_image(img, out_shape, device=0):
+    """the `scale` filter (downscaling) on the GPU; arrays [z, y, x]"""
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    out = np.empty(tuple(out_shape), np.float32)
+    isz = (ctypes.c_int * 3)(*(list(a.shape[::-1]) + [1] * (3 - a.ndim)))
+    osz = (ctypes.c_int * 3)(*(list(out.shape[::-1]) + [1] * (3 - out.ndim)))
+    check(lib().mgr_scale_image(a.ndim, isz, a.ctypes.data_as(_fp), osz, out.ctypes.data_as(_fp), int(device)))
+    return out
+
+
+def normalize_pair(src, ref, device=0):
+    s = np.ascontiguousarray(src, dtype=np.float32)
+    r = np.ascontiguousarray(ref, dtype=np.float32)
+    so, ro = np.empty_like(s), np.empty_like(r)
+    m, sg, ok = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    check(lib().mgr_normalize_pair(s.ctypes.data_as(_fp), r.ctypes.data_as(_fp), s.size, so.ctypes.data_as(_fp),
+                                   ro.ctypes.data_as(_fp), ctypes.byref(m), ctypes.byref(sg), ctypes.byref(ok),
+                                   int(device)))
+    return bool(ok.value), so, ro, m.value, sg.value

@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <functional>
@@ -1394,3 +1396,434 @@ void orc_level_force(OrcLevel *lvl, const double *params, float *force) { lvl->i
 void orc_level_translate(OrcLevel *lvl, const float *force, double *g) { lvl->impl->translate(force, g); }
 
 }  // extern "C"
+
+/* ===================================================================== */
+/* registration driver (TNonrigidRegisterImpl::run and its helpers)       */
+/* ===================================================================== */
+namespace {
+
+/* Binomial "gauss:w=" kernel (mia/core/spacialkernel/gauss.cc:27-57) and
+   its half-sample symmetric application (gauss.cc:72-137), restated as
+   out[i] = sum_j mask[j] * in[reflect(i - w + j)]. */
+std::vector<double> gauss_mask(int w)
+{
+    const int n = 2 * w + 1;
+    std::vector<double> k(n, 0.0), tmp(n, 0.0);
+    k[0] = 1.0;
+    if (n > 1) k[1] = 1.0;
+    for (int i = 2; i < n; ++i) {
+        k[i] = 1.0;
+        for (int j = 1; j < i; ++j) tmp[j] = k[j - 1] + k[j];
+        for (int j = 1; j < i; ++j) k[j] = tmp[j];
+    }
+    const double norm = std::pow(2.0, n - 1);
+    for (double &v : k) v /= norm;
+    return k;
+}
+
+/* C1DScalar (mia/core/scaler1d.cc): copy when the size is kept, else
+   gauss smoothing, mirror prefilter and cubic B-spline sampling at i*dx */
+void scale_line(const std::vector<double> &in, std::vector<double> &out)
+{
+    const int n = int(in.size()), m = int(out.size());
+    if (n == m) {
+        out = in;
+        return;
+    }
+    const double scale = double(m - 1) / double(n - 1);
+    const int w = int(std::floor(1.0 / scale + 0.5));
+    const std::vector<double> mask = gauss_mask(w);
+    std::vector<double> c(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        double h = 0.0;
+        for (int j = 0; j < 2 * w + 1; ++j) {
+            int k = i - w + j;
+            if (k < 0) k = -k - 1;
+            if (k >= n) k = 2 * n - 1 - k;
+            h += mask[j] * in[k];
+        }
+        c[i] = h;
+    }
+    filter_line(c.data(), n);
+    const double dx = 1.0 / scale;
+    for (int i = 0; i < m; ++i) {
+        const double x = double(i) * dx;
+        const int ix = fastfloor(x);
+        double wt[4];
+        weights3(x - ix, wt);
+        int id[4];
+        for (int q = 0; q < 4; ++q) id[q] = ix - 1 + q;
+        if (id[0] < 0 || id[3] >= n)
+            for (int q = 0; q < 4; ++q) id[q] = mirror_fold(id[q], n);
+        double v = 0.0;
+        for (int q = 0; q < 4; ++q) v += wt[q] * c[id[q]];
+        out[i] = v;
+    }
+}
+
+/* C3DScale::operator() / do_scale (mia/3d/filter/scale.cc:30-118),
+   C2DScale (mia/2d/filter/scale.cc:50-90): x, y, z passes over double
+   temporaries, float result */
+void scale_image_cpu(const float *in, int dim, const int is[3], float *out, const int os[3])
+{
+    const int nx = is[0], ny = is[1], nz = dim == 3 ? is[2] : 1;
+    const int mx = os[0], my = os[1], mz = dim == 3 ? os[2] : 1;
+    if (nx == mx && ny == my && nz == mz) {
+        std::copy(in, in + size_t(nx) * ny * nz, out);
+        return;
+    }
+    std::vector<double> t1(size_t(mx) * ny * nz), t2(size_t(mx) * my * nz);
+    std::vector<double> a, b;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            a.assign(in + (size_t(z) * ny + y) * nx, in + (size_t(z) * ny + y + 1) * nx);
+            b.assign(mx, 0.0);
+            scale_line(a, b);
+            std::copy(b.begin(), b.end(), t1.begin() + (size_t(z) * ny + y) * mx);
+        }
+    for (int z = 0; z < nz; ++z)
+        for (int x = 0; x < mx; ++x) {
+            a.resize(ny);
+            for (int y = 0; y < ny; ++y) a[y] = t1[(size_t(z) * ny + y) * mx + x];
+            b.assign(my, 0.0);
+            scale_line(a, b);
+            for (int y = 0; y < my; ++y) t2[(size_t(z) * my + y) * mx + x] = b[y];
+        }
+    if (dim == 2) {
+        for (size_t i = 0; i < size_t(mx) * my; ++i) out[i] = float(t2[i]);
+        return;
+    }
+    for (int y = 0; y < my; ++y)
+        for (int x = 0; x < mx; ++x) {
+            a.resize(nz);
+            for (int z = 0; z < nz; ++z) a[z] = t2[(size_t(z) * my + y) * mx + x];
+            b.assign(mz, 0.0);
+            scale_line(a, b);
+            for (int z = 0; z < mz; ++z) out[(size_t(z) * my + y) * mx + x] = float(b[z]);
+        }
+}
+
+/* FScaleFilterCreator + the "convert:repn=float,map=linear" filter
+   (mia/template/nonrigidregister.cxx:147-184, mia/template/convert.cxx:
+   78-92): a and b are written with the stream's default precision */
+bool normalize_cpu(const float *s, const float *r, size_t n, float *so, float *ro, double *mean_o,
+                   double *sigma_o)
+{
+    double sum = 0.0, sum2 = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const double fa = s[i], fb = r[i];
+        sum += fa + fb;
+        sum2 += fa * fa + fb * fb;
+    }
+    const double nn = 2.0 * double(n);
+    const double mean = sum / nn;
+    const double sigma = std::sqrt((sum2 - sum * sum / nn) / (nn - 1));
+    if (mean_o) *mean_o = mean;
+    if (sigma_o) *sigma_o = sigma;
+    if (sigma == 0.0) return false;
+    char buf[64];
+    snprintf(buf, sizeof buf, "%g", -mean / sigma);
+    const long double b = std::strtold(buf, nullptr);
+    snprintf(buf, sizeof buf, "%g", 1.0 / sigma);
+    const long double a = std::strtold(buf, nullptr);
+    for (size_t i = 0; i < n; ++i) {
+        so[i] = float(a * (long double)s[i] + b);
+        ro[i] = float(a * (long double)r[i] + b);
+    }
+    return true;
+}
+
+/* refine(): grid size (mia/3d/transform/spline.cc:363-364) */
+int refine_csize_cpu(int size, float rate) { return int((float(size) + rate - 1.0f) / rate) + 2; }
+
+/* refine() interpolation (spline.cc:360-396, 2D spline.cc:318-353) with a
+   vector-valued T3DConvoluteInterpolator: double coefficients, clamp to the
+   componentwise min/max (min set to 0 only if all components are > 0) */
+bool refine_cpu(int dim, const int nco[3], const int ncn[3], std::vector<double> &p)
+{
+    bool any = false;
+    for (int k = 0; k < dim; ++k)
+        if (ncn[k] > nco[k]) any = true;
+    if (!any) return false;
+    const int ox = nco[0], oy = nco[1], oz = dim == 3 ? nco[2] : 1;
+    const size_t no = size_t(ox) * oy * oz;
+    std::vector<double> comp(no);
+    std::vector<std::vector<double>> coef(dim);
+    float mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    Pool pool;
+    for (int c = 0; c < dim; ++c) {
+        for (size_t i = 0; i < no; ++i) comp[i] = double(float(p[i * dim + c]));
+        mn[c] = mx[c] = float(comp[0]);
+        for (size_t i = 1; i < no; ++i) {
+            mn[c] = std::min(mn[c], float(comp[i]));
+            mx[c] = std::max(mx[c], float(comp[i]));
+        }
+        prefilter_nd(comp.data(), ox, oy, oz, pool);
+        coef[c] = comp;
+    }
+    bool allpos = true;
+    for (int c = 0; c < dim; ++c)
+        if (!(0.0f < mn[c])) allpos = false;
+    if (allpos)
+        for (int c = 0; c < dim; ++c) mn[c] = 0.0f;
+    const int nx = ncn[0], ny = ncn[1], nz = dim == 3 ? ncn[2] : 1;
+    float dxs[3] = {1, 1, 1};
+    for (int k = 0; k < dim; ++k) dxs[k] = float(nco[k] - 3) / float(ncn[k] - 3);
+    std::vector<double> out(size_t(nx) * ny * nz * dim);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const float P[3] = {dxs[0] * (float(x) - 1.0f) + 1.0f, dxs[1] * (float(y) - 1.0f) + 1.0f,
+                                    dxs[2] * (float(z) - 1.0f) + 1.0f};
+                int idx[3][4];
+                double wt[3][4];
+                const int width[3] = {ox, oy, oz};
+                for (int k = 0; k < 3; ++k) {
+                    if (k >= dim) {
+                        idx[k][0] = 0;
+                        wt[k][0] = 1.0;
+                        continue;
+                    }
+                    const int s = start_weights(double(P[k]), wt[k]);
+                    for (int q = 0; q < 4; ++q) {
+                        int i = s + q;
+                        if (s < 0 || s + 3 >= width[k]) i = mirror_fold(i, width[k]);
+                        idx[k][q] = i;
+                    }
+                }
+                const int kzn = dim == 3 ? 4 : 1;
+                for (int c = 0; c < dim; ++c) {
+                    double r = 0.0;
+                    for (int kz = 0; kz < kzn; ++kz) {
+                        double ry = 0.0;
+                        for (int ky = 0; ky < 4; ++ky) {
+                            double rx = 0.0;
+                            for (int kx = 0; kx < 4; ++kx)
+                                rx += wt[0][kx] * coef[c][(size_t(idx[2][kz]) * oy + idx[1][ky]) * ox + idx[0][kx]];
+                            ry += wt[1][ky] * rx;
+                        }
+                        r += wt[2][kz] * ry;
+                    }
+                    r = (r >= mn[c]) ? ((r <= mx[c]) ? r : mx[c]) : mn[c];
+                    out[((size_t(z) * ny + y) * nx + x) * dim + c] = double(float(r));
+                }
+            }
+    p.swap(out);
+    return true;
+}
+
+typedef std::function<double(const std::vector<double> &, std::vector<double> &)> Fdf;
+
+/* GSL steepest descent (multimin/steepest_descent.c) as driven by
+   CGSLFDFMinimizer::do_run (mia/core/minimizer/gsl.cc:122-156) */
+double run_gsl_sd(std::vector<double> &x, const OrcMinimizer &mz, const Fdf &fdf, int *evals)
+{
+    const size_t n = x.size();
+    std::vector<double> g(n), x1(n), g1(n);
+    double f = fdf(x, g);
+    int ne = 1;
+    double step = mz.step;
+    int iter = 0;
+    for (;;) {
+        ++iter;
+        double gn = 0.0;
+        for (double v : g) gn += v * v;
+        gn = std::sqrt(gn);
+        if (gn == 0.0) break;
+        bool failed = false, noprog = false;
+        double f1 = 0.0;
+        for (int trial = 0;; ++trial) {
+            const double a = -step / gn;
+            bool eq = true;
+            for (size_t i = 0; i < n; ++i) {
+                x1[i] = x[i] + a * g[i];
+                if (x1[i] != x[i]) eq = false;
+            }
+            if (eq || trial >= 2000) {
+                noprog = true;
+                break;
+            }
+            f1 = fdf(x1, g1);
+            ++ne;
+            if (f1 > f) {
+                failed = true;
+                step *= mz.tol;
+                continue;
+            }
+            break;
+        }
+        if (noprog) break;
+        step *= failed ? mz.tol : 2.0;
+        x.swap(x1);
+        g.swap(g1);
+        f = f1;
+        double gn2 = 0.0;
+        for (double v : g) gn2 += v * v;
+        if (std::sqrt(gn2) < mz.eps || iter >= mz.maxiter) break;
+    }
+    if (evals) *evals += ne;
+    return f;
+}
+
+/* CGDSQMinimizer::do_run (mia/core/minimizer/gdsq.cc:60-122) */
+double run_gdsq(std::vector<double> &x, const OrcMinimizer &mz, const Fdf &fdf, int *evals)
+{
+    auto test_tol = [](const std::vector<double> &v, double tol, int cause) {
+        for (double e : v)
+            if (std::fabs(e) >= tol) return 0;
+        return cause;
+    };
+    const size_t n = x.size();
+    std::vector<double> g(n), gt(n), xw(x);
+    double f_old = fdf(xw, g);
+    int ne = 1;
+    double step = mz.step;
+    unsigned iter = 0;
+    int success = test_tol(g, mz.xtol, 1);
+    while (iter++ < unsigned(mz.maxiter) && step > mz.min_step && !success) {
+        for (size_t i = 0; i < n; ++i) xw[i] += -step * g[i];
+        const double f = fdf(xw, gt);
+        ++ne;
+        if (f < f_old) {
+            for (size_t i = 0; i < n; ++i) g[i] *= -step;
+            double sum = 0.0;
+            for (size_t i = 0; i < n; ++i) sum += g[i] * gt[i];
+            const double aux = f_old - f + sum;
+            if (aux <= 0.0) step *= mz.scale;
+            else {
+                double nn = 0.0;
+                for (double v : g) nn += v * v;
+                step = 0.5 * std::sqrt(nn) / aux;
+            }
+            x = xw;
+            g = gt;
+            const double frel = f_old - f;
+            f_old = f;
+            success |= test_tol(gt, mz.gtol, 2);
+            if (frel < mz.ftolr) success |= 4;
+        } else {
+            xw = x;
+            step /= mz.scale;
+        }
+        success |= test_tol(g, mz.xtol / step, 1);
+    }
+    if (evals) *evals += ne;
+    return f_old;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_normalize_pair(const float *src, const float *ref, size_t n, float *so, float *ro, double *mean,
+                       double *sigma)
+{
+    return normalize_cpu(src, ref, n, so, ro, mean, sigma) ? 1 : 0;
+}
+
+void orc_scale_image(const float *in, int dim, const int in_size[3], float *out, const int out_size[3])
+{
+    scale_image_cpu(in, dim, in_size, out, out_size);
+}
+
+int orc_refine(int dim, const int nco[3], const int ncn[3], const double *p, double *out, size_t max_out)
+{
+    std::vector<double> v(p, p + size_t(nco[0]) * nco[1] * (dim == 3 ? nco[2] : 1) * dim);
+    if (!refine_cpu(dim, nco, ncn, v)) return 0;
+    if (v.size() > max_out) return -1;
+    std::copy(v.begin(), v.end(), out);
+    return int(v.size());
+}
+
+int orc_register(const OrcLevelDesc *desc, int levels, const OrcMinimizer *mz, const float *src,
+                 const float *ref, double *params_out, int max_params, int csize_out[3], double *final_cost,
+                 int *evals_out)
+{
+    const int dim = desc->dim;
+    const int fs[3] = {desc->size[0], desc->size[1], dim == 3 ? desc->size[2] : 1};
+    const size_t nf = size_t(fs[0]) * fs[1] * fs[2];
+    std::vector<float> sn(nf), rn(nf);
+    int evals = 0;
+    double cost = 0.0;
+    int cs[3] = {1, 1, 1};
+    std::vector<double> p;
+    if (!normalize_cpu(src, ref, nf, sn.data(), rn.data(), nullptr, nullptr)) {
+        for (int k = 0; k < dim; ++k) cs[k] = Spline<RefP>::csize_from_rate(fs[k], desc->rate[k]);
+        p.assign(size_t(cs[0]) * cs[1] * cs[2] * dim, 0.0);
+    } else {
+        int prev[3] = {0, 0, 0};
+        for (int shift = levels - 1; shift >= 0; --shift) {
+            int sz[3] = {1, 1, 1};
+            for (int k = 0; k < dim; ++k) sz[k] = fs[k] / (1 << shift);
+            if (shift == levels - 1) {
+                for (int k = 0; k < dim; ++k) cs[k] = Spline<RefP>::csize_from_rate(sz[k], desc->rate[k]);
+                p.assign(size_t(cs[0]) * cs[1] * cs[2] * dim, 0.0);
+            } else {
+                /* do_upscale (spline.cc:399-412; 2D :356-370) */
+                float mxs[3];
+                for (int k = 0; k < dim; ++k)
+                    mxs[k] = dim == 3 ? float(sz[k]) / float(prev[k]) : (float(sz[k]) - 1) / (float(prev[k]) - 1);
+                for (size_t i = 0; i < p.size(); ++i) p[i] = double(mxs[i % dim] * float(p[i]));
+            }
+            const size_t n = size_t(sz[0]) * sz[1] * sz[2];
+            std::vector<float> sl(n), rl(n);
+            scale_image_cpu(sn.data(), dim, fs, sl.data(), sz);
+            scale_image_cpu(rn.data(), dim, fs, rl.data(), sz);
+            for (int pass = 0; pass < 2; ++pass) {
+                OrcLevelDesc d = *desc;
+                for (int k = 0; k < 3; ++k) {
+                    d.size[k] = sz[k];
+                    d.csize[k] = cs[k];
+                }
+                OrcLevel *lv = orc_level_create(&d);
+                orc_level_set_images(lv, sl.data(), rl.data());
+                Fdf fdf = [&](const std::vector<double> &x, std::vector<double> &g) {
+                    std::vector<double> gp(g.size());
+                    double ci = 0, cp = 0;
+                    orc_level_evaluate(lv, x.data(), g.data(), gp.data(), &ci, &cp);
+                    for (size_t i = 0; i < g.size(); ++i) g[i] += gp[i];
+                    return ci + cp;
+                };
+                cost = (mz->kind == ORC_MIN_GDSQ) ? run_gdsq(p, *mz, fdf, &evals) : run_gsl_sd(p, *mz, fdf, &evals);
+                orc_level_destroy(lv);
+                for (double &v : p) v = double(float(v));
+                if (pass == 1) break;
+                int ncn[3] = {1, 1, 1};
+                for (int k = 0; k < dim; ++k) ncn[k] = refine_csize_cpu(sz[k], desc->rate[k]);
+                if (!refine_cpu(dim, cs, ncn, p)) break;
+                for (int k = 0; k < 3; ++k) cs[k] = ncn[k];
+            }
+            for (int k = 0; k < 3; ++k) prev[k] = sz[k];
+        }
+    }
+    if (int(p.size()) > max_params) return -1;
+    std::copy(p.begin(), p.end(), params_out);
+    for (int k = 0; k < 3; ++k) csize_out[k] = cs[k];
+    if (final_cost) *final_cost = cost;
+    if (evals_out) *evals_out = evals;
+    return int(p.size());
+}
+
+}  // extern "C"
+
+extern "C" {
+/* The analytic problem of the reference's gdsq test
+   (mia/core/minimizer/test_gdsq.cc:25-80):
+   f = p2 (x - p0)^2 + p3 (y - p1)^2 + p4 with p = (1, 2, 10, 20, 30). */
+double orc_minimize_test_problem(const OrcMinimizer *mz, double x[2], int *evals)
+{
+    const double pp[5] = {1.0, 2.0, 10.0, 20.0, 30.0};
+    Fdf fdf = [&](const std::vector<double> &v, std::vector<double> &g) {
+        g[0] = 2.0 * pp[2] * (v[0] - pp[0]);
+        g[1] = 2.0 * pp[3] * (v[1] - pp[1]);
+        return pp[2] * (v[0] - pp[0]) * (v[0] - pp[0]) + pp[3] * (v[1] - pp[1]) * (v[1] - pp[1]) + pp[4];
+    };
+    std::vector<double> v(x, x + 2);
+    int ne = 0;
+    const double f = (mz->kind == ORC_MIN_GDSQ) ? run_gdsq(v, *mz, fdf, &ne) : run_gsl_sd(v, *mz, fdf, &ne);
+    x[0] = v[0];
+    x[1] = v[1];
+    if (evals) *evals = ne;
+    return f;
+}
+}

@@ -89,6 +89,31 @@ void      orc_level_displacement(OrcLevel *lvl, const double *params, float *u);
 void      orc_level_force(OrcLevel *lvl, const double *params, float *force);
 void      orc_level_translate(OrcLevel *lvl, const float *force, double *g);
 
+/* ---- registration driver -------------------------------------------- */
+enum { ORC_MIN_GSL_SD = 0, ORC_MIN_GDSQ = 1 };
+typedef struct {
+    int    kind;
+    int    maxiter;
+    double step;
+    double tol;       /* gsl: step factor after a failed trial */
+    double eps;       /* gsl: stop when |g| < eps */
+    double scale;     /* gdsq */
+    double xtol, gtol, ftolr, min_step;   /* gdsq */
+} OrcMinimizer;
+
+int  orc_normalize_pair(const float *src, const float *ref, size_t n, float *src_out, float *ref_out,
+                        double *mean, double *sigma);
+void orc_scale_image(const float *in, int dim, const int in_size[3], float *out, const int out_size[3]);
+int  orc_refine(int dim, const int nc_old[3], const int nc_new[3], const double *params, double *out,
+                size_t max_out);
+/* TNonrigidRegisterImpl::run for the spline transformation; returns the
+   number of parameters written or -1 */
+int  orc_register(const OrcLevelDesc *desc, int levels, const OrcMinimizer *mz, const float *src,
+                  const float *ref, double *params_out, int max_params, int csize_out[3],
+                  double *final_cost, int *evals_out);
+/* the minimizers on the analytic problem of the reference's gdsq test */
+double orc_minimize_test_problem(const OrcMinimizer *mz, double x[2], int *evals);
+
 #ifdef __cplusplus
 }
 #endif

@@ -313,3 +313,110 @@ class Level:
         g = np.zeros(self.nparams)
         lib().orc_level_translate(self.h, f.ctypes.data_as(_fp), g.ctypes.data_as(_dp))
         return g
+
+
+# ---- registration driver --------------------------------------------------
+MIN_GSL_SD, MIN_GDSQ = 0, 1
+
+
+class Minimizer(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("maxiter", ctypes.c_int),
+        ("step", ctypes.c_double),
+        ("tol", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("scale", ctypes.c_double),
+        ("xtol", ctypes.c_double),
+        ("gtol", ctypes.c_double),
+        ("ftolr", ctypes.c_double),
+        ("min_step", ctypes.c_double),
+    ]
+
+
+def minimizer(kind="gsl", maxiter=100, step=None, tol=0.1, eps=0.01, scale=2.0, xtol=0.0, gtol=0.0, ftolr=0.0,
+              min_step=1e-6):
+    m = Minimizer()
+    m.kind = MIN_GDSQ if kind == "gdsq" else MIN_GSL_SD
+    m.maxiter = int(maxiter)
+    m.step = float(step if step is not None else 0.1)
+    m.tol, m.eps, m.scale = float(tol), float(eps), float(scale)
+    m.xtol, m.gtol, m.ftolr, m.min_step = float(xtol), float(gtol), float(ftolr), float(min_step)
+    return m
+
+
+def _drv():
+    L = lib()
+    if not getattr(L, "_drv_ready", False):
+        L.orc_normalize_pair.restype = ctypes.c_int
+        L.orc_normalize_pair.argtypes = [_fp, _fp, ctypes.c_size_t, _fp, _fp, _dp, _dp]
+        L.orc_scale_image.argtypes = [_fp, ctypes.c_int, _ip, _fp, _ip]
+        L.orc_refine.restype = ctypes.c_int
+        L.orc_refine.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_size_t]
+        L.orc_register.restype = ctypes.c_int
+        L.orc_register.argtypes = [ctypes.POINTER(LevelDesc), ctypes.c_int, ctypes.POINTER(Minimizer), _fp, _fp,
+                                   _dp, ctypes.c_int, _ip, _dp, _ip]
+        L.orc_minimize_test_problem.restype = ctypes.c_double
+        L.orc_minimize_test_problem.argtypes = [ctypes.POINTER(Minimizer), _dp, _ip]
+        L._drv_ready = True
+    return L
+
+
+def normalize_pair(src, ref):
+    s, r = _f(src), _f(ref)
+    so, ro = np.empty_like(s), np.empty_like(r)
+    m, sg = ctypes.c_double(), ctypes.c_double()
+    ok = _drv().orc_normalize_pair(s.ctypes.data_as(_fp), r.ctypes.data_as(_fp), s.size, so.ctypes.data_as(_fp),
+                                   ro.ctypes.data_as(_fp), ctypes.byref(m), ctypes.byref(sg))
+    return bool(ok), so, ro, m.value, sg.value
+
+
+def scale_image(img, out_shape):
+    img = _f(img)
+    out = np.empty(tuple(out_shape), np.float32)
+    _drv().orc_scale_image(img.ctypes.data_as(_fp), img.ndim, _size3(img.shape[::-1]), out.ctypes.data_as(_fp),
+                           _size3(out.shape[::-1]))
+    return out
+
+
+def refine(dim, nc_old, nc_new, params):
+    p = _d(params)
+    out = np.empty(int(np.prod(nc_new)) * dim)
+    n = _drv().orc_refine(dim, _size3(nc_old), _size3(nc_new), p.ctypes.data_as(_dp), out.ctypes.data_as(_dp),
+                          out.size)
+    return None if n == 0 else out
+
+
+def minimize_test_problem(mz, x0=(5.0, 7.0)):
+    x = np.array(x0, dtype=np.float64)
+    ne = ctypes.c_int()
+    f = _drv().orc_minimize_test_problem(ctypes.byref(mz), x.ctypes.data_as(_dp), ctypes.byref(ne))
+    return f, x, ne.value
+
+
+def register(src, ref, rate, levels, mz, cost="ssd", penalty_weight=None, div=1.0, curl=1.0, ssd_norm=False,
+             cost_weight=1.0, penalty_norm=False, threads=1):
+    """TNonrigidRegisterImpl::run: returns (params, csize, final_cost, evaluations)"""
+    s, r = _f(src), _f(ref)
+    d = LevelDesc()
+    d.dim = s.ndim
+    d.size = _size3(s.shape[::-1])
+    d.csize = _size3([0] * d.dim)
+    rr = rate if hasattr(rate, "__len__") else [rate] * d.dim
+    d.rate = (ctypes.c_float * 3)(*(list(rr) + [1.0] * (3 - len(rr))))
+    d.cost = COST_NCC if cost == "ncc" else COST_SSD
+    d.ssd_norm, d.cost_weight = int(ssd_norm), cost_weight
+    d.has_penalty = int(penalty_weight is not None)
+    d.pen_weight = penalty_weight or 0.0
+    d.pen_div, d.pen_curl, d.pen_norm = div, curl, int(penalty_norm)
+    d.precision, d.threads = PREC_REF, threads
+    maxp = 1 << 24
+    out = np.empty(maxp)
+    cs = (ctypes.c_int * 3)()
+    fc, ne = ctypes.c_double(), ctypes.c_int()
+    n = _drv().orc_register(ctypes.byref(d), int(levels), ctypes.byref(mz), s.ctypes.data_as(_fp),
+                            r.ctypes.data_as(_fp), out.ctypes.data_as(_dp), maxp, cs, ctypes.byref(fc),
+                            ctypes.byref(ne))
+    if n < 0:
+        raise RuntimeError("orc_register failed")
+    return out[:n].copy(), tuple(cs[: d.dim]), fc.value, ne.value

@@ -188,7 +188,7 @@ def test_tiles_and_determinism():
     from mia_gb300 import synth
     p = synth.smooth_params(g.csize, 1.0, seed=3)
     ref_out = None
-    for tile in ((32, 8, 8), (64, 4, 4), (32, 16, 2), (96, 8, 8)):
+    for tile in ((32, 8, 8), (64, 4, 4), (32, 16, 4), (32, 4, 4), (64, 8, 4)):
         g.set_path("split", tile)
         out = g.evaluate(p)
         check_eval(g, o, o64, p, "split")
