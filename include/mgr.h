@@ -193,6 +193,32 @@ mgr_status mgr_register(const mgr_level_desc *desc, int levels, const mgr_minimi
                         double *params_out, size_t max_params, int csize_out[3],
                         double *final_cost, int *evaluations);
 
+/* Registration of many pairs at once; replaces the per-pair loop of the
+   series programs (src/2dmyoset-all2one-nonrigid.cc:124-190,
+   src/3dmany2one-nonrigid.cc:118-187), which run one mgr_register-like
+   registration per pair in host threads.  All pairs must have the same
+   dimension, cost and penalty; sizes may differ.  Each pair follows the same
+   levels / refine / minimizer sequence as mgr_register, but the minimizers
+   run as device state machines and one step evaluates every unfinished
+   pair with one launch per kernel over a (pair, tile) work list; with
+   `use_graphs` the steps of each level are captured as a CUDA graph.
+   csize_out holds 3 ints per pair; params_out[p] receives max_params[p]
+   doubles at most. */
+mgr_status mgr_register_batch(int npairs, const mgr_level_desc *descs, int levels,
+                              const mgr_minimizer_desc *mz, const float *const *srcs,
+                              const float *const *refs, int device, int use_graphs,
+                              double *const *params_out, const size_t *max_params, int *csize_out,
+                              double *final_costs, int *evaluations);
+
+/* mgr_register_batch with the images already in device memory (device
+   pointers on `device`); no counterpart in the reference, which holds its
+   images in host memory. */
+mgr_status mgr_register_batch_device(int npairs, const mgr_level_desc *descs, int levels,
+                                     const mgr_minimizer_desc *mz, const float *const *d_srcs,
+                                     const float *const *d_refs, int device, int use_graphs,
+                                     double *const *params_out, const size_t *max_params, int *csize_out,
+                                     double *final_costs, int *evaluations);
+
 /* Replaces: the `scale` filter that builds a multiresolution level
    (C3DScale::operator(), mia/3d/filter/scale.cc:95-118; C2DScale,
    mia/2d/filter/scale.cc:50-90); downscaling only.  Host images, run on

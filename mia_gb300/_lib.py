@@ -40,6 +40,10 @@ SIGNATURES = {
     "mgr_translate3d_noalloc": (ctypes.c_int, [_ip, _ip, _vp, _vp, _vp]),
     "mgr_register": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _fp, _fp, ctypes.c_int, ctypes.c_int, _dp,
                                     ctypes.c_size_t, _ip, _dp, _ip]),
+    "mgr_register_batch": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int,
+                                          ctypes.c_int, _vp, _vp, _ip, _dp, _ip]),
+    "mgr_register_batch_device": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int,
+                                                 ctypes.c_int, _vp, _vp, _ip, _dp, _ip]),
     "mgr_scale_image": (ctypes.c_int, [ctypes.c_int, _ip, _fp, _ip, _fp, ctypes.c_int]),
     "mgr_normalize_pair": (ctypes.c_int, [_fp, _fp, ctypes.c_size_t, _fp, _fp, _dp, _dp, _ip, ctypes.c_int]),
 }

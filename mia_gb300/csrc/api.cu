@@ -2,198 +2,68 @@
 // memory, table upload and the evaluation pipelines.
 #include <atomic>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "../../include/mgr.h"
-#include "mgr_kernels.hh"
-#include "tables.hh"
+#include "level.hh"
+#include "trace.hh"
 
 namespace mgr {
 
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void count_launch_adjust(unsigned long long value) { g_launches.store(value); }
 
 static thread_local std::string g_err;
 void set_last_error(const std::string &msg) { g_err = msg; }
 
-struct CudaError : std::runtime_error {
-    using std::runtime_error::runtime_error;
+// phase trace (MGR_TRACE=1)
+namespace {
+struct PhaseSum {
+    std::string name;
+    double ms;
+    long n;
 };
-struct StateError : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
+std::mutex g_trace_mu;
+std::vector<PhaseSum> g_trace;
+}  // namespace
 
-static void ck(cudaError_t e, const char *what)
+bool trace_enabled()
 {
-    if (e != cudaSuccess) {
-        std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-        if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
-        throw CudaError(m);
-    }
+    static const bool on = [] {
+        const char *e = std::getenv("MGR_TRACE");
+        return e && *e && std::strcmp(e, "0") != 0;
+    }();
+    return on;
 }
 
-template <class T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t n = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    void alloc(size_t count)
-    {
-        if (count <= n && p) return;
-        release();
-        if (count == 0) return;
-        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
-        n = count;
-    }
-    void upload(const std::vector<T> &h, cudaStream_t st)
-    {
-        alloc(h.size());
-        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
-    }
-};
-
-struct AxisDev {
-    AxisHost h;
-    DevBuf<int> fs, as, rows, ftile0, atile0, gtile;
-    DevBuf<float> fw, aw;
-    void upload(cudaStream_t st)
-    {
-        fs.upload(h.fs, st);
-        as.upload(h.as, st);
-        rows.upload(h.rows, st);
-        ftile0.upload(h.ftile0, st);
-        atile0.upload(h.atile0, st);
-        gtile.upload(h.gtile, st);
-        fw.upload(h.fw, st);
-        aw.upload(h.aw, st);
-    }
-    Axis view() const
-    {
-        Axis a;
-        a.fs = fs.p;
-        a.fw = reinterpret_cast<const float4 *>(fw.p);
-        a.as = as.p;
-        a.aw = reinterpret_cast<const float4 *>(aw.p);
-        a.rows = reinterpret_cast<const int2 *>(rows.p);
-        a.ftile0 = ftile0.p;
-        a.atile0 = atile0.p;
-        a.gtile = reinterpret_cast<const int2 *>(gtile.p);
-        a.n = h.n;
-        a.nc = h.nc;
-        a.t = h.t;
-        a.nt = h.nt;
-        a.fc = h.fc;
-        a.ac = h.ac;
-        return a;
-    }
-};
-
-}  // namespace mgr
-
-using namespace mgr;
-
-struct mgr_level {
-    mgr_level_desc d{};
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int n[3] = {1, 1, 1}, nc[3] = {1, 1, 1};
-    size_t N = 0, ncoef = 0, nparams = 0;
-    int path = MGR_PATH_SPLIT;
-    int tile[3] = {32, 8, 8};
-    AxisDev ax[3];
-    DevBuf<float> coef, ref, warped, minmax, partial, ptable, pen_val;
-    DevBuf<float2> mmpart;
-    DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means;
-    DevBuf<unsigned int> counters;
-    DevBuf<int> pen_rowptr, pen_col;
-    DevBuf<float> grid, force, tmp1, tmp2;   // plain path and standalone force/translate
-    int slot = 0;
-    double center_a = 0.0, center_b = 0.0;
-    bool images_set = false;
-    bool tables_valid = false;
-    bool timing = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    bool ev_recorded = false;
-    void record(int k)
-    {
-        if (timing) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");
-    }
-    ~mgr_level()
-    {
-        for (auto &e : ev)
-            if (e) cudaEventDestroy(e);
-    }
-
-    EvalArgs args() const
-    {
-        EvalArgs a{};
-        a.dim = d.dim;
-        for (int k = 0; k < 3; ++k) {
-            a.n[k] = n[k];
-            a.nc[k] = nc[k];
-            a.ax[k] = ax[k].view();
+void trace_add(const char *phase, double ms)
+{
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    for (auto &p : g_trace)
+        if (p.name == phase) {
+            p.ms += ms;
+            p.n += 1;
+            return;
         }
-        a.coef_img = coef.p;
-        a.ref = ref.p;
-        a.warped = warped.p;
-        a.minmax = minmax.p;
-        a.params = params.p;
-        a.cost = d.cost;
-        a.ssd_norm = d.ssd_norm;
-        a.cost_weight = d.cost_weight;
-        a.center_a = center_a;
-        a.center_b = center_b;
-        a.partial = partial.p;
-        a.slot = slot;
-        a.tile_sums = tile_sums.p;
-        a.counters = counters.p;
-        a.scalars = scalars.p;
-        a.has_penalty = d.has_penalty;
-        double prod = double(d.size[0]) * d.size[1] * (d.dim == 3 ? d.size[2] : 1);
-        a.pen_weight = d.pen_norm ? d.pen_weight / double(float(prod)) : d.pen_weight;
-        a.pen_equal_w = d.pen_div == d.pen_curl;
-        a.ptable = ptable.p;
-        a.pen_rowptr = pen_rowptr.p;
-        a.pen_col = pen_col.p;
-        a.pen_val = reinterpret_cast<const float4 *>(pen_val.p);
-        a.pen_part = pen_part.p;
-        a.grad_total = grad_total.p;
-        a.grad_image = nullptr;
-        a.grad_penalty = nullptr;
-        a.costs = costs.p;
-        return a;
-    }
+    g_trace.push_back({phase, ms, 1});
+}
 
-    void build_tables()
-    {
-        const int D = d.dim;
-        for (int k = 0; k < D; ++k) {
-            build_axis(ax[k].h, n[k], nc[k], tile[k]);
-            ax[k].upload(stream);
-        }
-        const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
-        slot = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
-        partial.alloc(size_t(ntiles) * slot);
-        const size_t plain_blocks = (N + 255) / 256;
-        tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5);
-        pen_part.alloc(size_t(gather_blocks(args())) + 1);
-        tables_valid = true;
-    }
-};
+void trace_report(const char *title)
+{
+    if (!trace_enabled()) return;
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    std::fprintf(stderr, "[mgr trace] %s\n", title);
+    for (auto &p : g_trace) std::fprintf(stderr, "  %-28s %10.3f ms  %6ld calls\n", p.name.c_str(), p.ms, p.n);
+    g_trace.clear();
+}
 
 static mgr_status fail(mgr_status s, const std::string &m)
 {
@@ -224,6 +94,10 @@ static void check_launch(const char *what)
 {
     ck(cudaGetLastError(), what);
 }
+
+}  // namespace mgr
+
+using namespace mgr;
 
 extern "C" {
 

@@ -1,0 +1,609 @@
+// batch.cu — registration of many image pairs at once (a perfusion series
+// against its reference frame, a cohort of 3D pairs; src/2dmyoset-all2one-
+// nonrigid.cc:124-190, src/3dmany2one-nonrigid.cc:118-187 run one
+// registration per pair in parallel host threads).
+//
+// All pairs advance in lock step.  One step evaluates the cost+gradient of
+// every unfinished pair at the point its minimizer proposes:
+//   k_min_propose  (one block per pair) the minimizer's next evaluation point
+//   warp, adjoint, gather of the split path over a work list of
+//                  (pair, tile) / (pair, block) items covering all pairs
+//   k_min_update   (one block per pair) the minimizer's decision
+// The minimizers (GSL steepest descent as CGSLFDFMinimizer drives it,
+// mia/core/minimizer/gsl.cc:122-156, and CGDSQMinimizer::do_run,
+// mia/core/minimizer/gdsq.cc:60-122) are state machines in device memory, so
+// a run of steps needs no host round trip and is captured once per level and
+// pass as a CUDA graph that is relaunched until every pair has finished.
+// Level transitions (scale filter, upscale, refine) follow
+// TNonrigidRegisterImpl::run (mia/template/nonrigidregister.cxx:193-296).
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mgr.h"
+#include "driver.hh"
+#include "level.hh"
+#include "pyramid.hh"
+#include "trace.hh"
+
+namespace mgr {
+
+void set_last_error(const std::string &msg);
+
+namespace {
+
+constexpr int MT = 256;
+
+struct MinState {
+    double f;       // cost at x
+    double step;
+    double f_old;   // gdsq
+    int iter;
+    int phase;      // 0: evaluate x0, 1: iterate
+    int failed;     // gsl: a trial failed in this iteration
+    int trials;     // gsl: trials in this iteration
+    int done;
+    int evals;
+    int success;    // gdsq stop flags
+    int status;     // 0 running/converged, 1 no progress, 2 max iterations
+};
+
+struct PairVec {
+    double *x, *g, *xt, *gt;
+    const double *costs;   // {image, penalty} at xt
+    int n;
+};
+
+__device__ double block_reduce_sum(double v, double *red)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < MT / 32; ++k) s += red[k];
+    __syncthreads();
+    if (threadIdx.x == 0) red[0] = s;
+    __syncthreads();
+    s = red[0];
+    __syncthreads();
+    return s;
+}
+
+__device__ int block_all(int pred, int *flag)
+{
+    if (threadIdx.x == 0) *flag = 1;
+    __syncthreads();
+    if (!pred) *flag = 0;
+    __syncthreads();
+    const int r = *flag;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(MT) k_min_propose(MinState *st, const PairVec *vec, mgr_minimizer_desc mz,
+                                                    int *active)
+{
+    __shared__ double red[MT / 32];
+    __shared__ int flag;
+    const int p = blockIdx.x;
+    MinState &s = st[p];
+    const PairVec v = vec[p];
+    if (s.done) {
+        if (threadIdx.x == 0) active[p] = 0;
+        return;
+    }
+    if (s.phase == 0) {
+        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = v.x[i];
+        if (threadIdx.x == 0) active[p] = 1;
+        return;
+    }
+    if (mz.kind == MGR_MIN_GSL_SD) {
+        double q = 0.0;
+        for (int i = threadIdx.x; i < v.n; i += MT) q += v.g[i] * v.g[i];
+        const double gnorm = sqrt(block_reduce_sum(q, red));
+        if (gnorm == 0.0 || s.trials >= 2000) {
+            if (threadIdx.x == 0) {
+                s.done = 1;
+                s.status = 1;
+                active[p] = 0;
+            }
+            return;
+        }
+        const double a = -s.step / gnorm;
+        int same = 1;
+        for (int i = threadIdx.x; i < v.n; i += MT) {
+            const double x1 = __dadd_rn(v.x[i], __dmul_rn(a, v.g[i]));
+            v.xt[i] = x1;
+            if (x1 != v.x[i]) same = 0;
+        }
+        if (block_all(same, &flag)) {
+            if (threadIdx.x == 0) {
+                s.done = 1;
+                s.status = 1;
+                active[p] = 0;
+            }
+            return;
+        }
+        if (threadIdx.x == 0) {
+            s.trials += 1;
+            active[p] = 1;
+        }
+    } else {
+        // while (iter++ < maxiter && step > min_step && !success)
+        const bool go = (s.iter < mz.maxiter) && (s.step > mz.min_step) && !s.success;
+        __syncthreads();
+        if (threadIdx.x == 0) s.iter += 1;
+        if (!go) {
+            if (threadIdx.x == 0) {
+                s.done = 1;
+                active[p] = 0;
+            }
+            return;
+        }
+        const double ms = -s.step;
+        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = __dadd_rn(v.xt[i], __dmul_rn(ms, v.g[i]));
+        if (threadIdx.x == 0) active[p] = 1;
+    }
+}
+
+__global__ void __launch_bounds__(MT) k_min_update(MinState *st, const PairVec *vec, mgr_minimizer_desc mz,
+                                                   const int *active)
+{
+    __shared__ double red[MT / 32];
+    __shared__ int flag;
+    const int p = blockIdx.x;
+    if (!active[p]) return;
+    MinState &s = st[p];
+    const PairVec v = vec[p];
+    const double fe = v.costs[0] + v.costs[1];
+    if (s.phase == 0) {
+        for (int i = threadIdx.x; i < v.n; i += MT) v.g[i] = v.gt[i];
+        int small = 1;
+        if (mz.kind == MGR_MIN_GDSQ)
+            for (int i = threadIdx.x; i < v.n; i += MT)
+                if (fabs(v.gt[i]) >= mz.xtol) small = 0;
+        const int all_small = block_all(small, &flag);
+        if (threadIdx.x == 0) {
+            s.f = fe;
+            s.f_old = fe;
+            s.phase = 1;
+            s.evals += 1;
+            if (mz.kind == MGR_MIN_GDSQ && all_small) s.success |= 1;
+        }
+        return;
+    }
+    if (mz.kind == MGR_MIN_GSL_SD) {
+        if (fe > s.f) {
+            if (threadIdx.x == 0) {
+                s.evals += 1;
+                s.failed = 1;
+                s.step *= mz.tol;
+            }
+            return;
+        }
+        double q = 0.0;
+        for (int i = threadIdx.x; i < v.n; i += MT) {
+            v.x[i] = v.xt[i];
+            v.g[i] = v.gt[i];
+            q += v.gt[i] * v.gt[i];
+        }
+        const double gn = sqrt(block_reduce_sum(q, red));
+        if (threadIdx.x == 0) {
+            s.evals += 1;
+            s.step *= s.failed ? mz.tol : 2.0;
+            s.f = fe;
+            s.failed = 0;
+            s.trials = 0;
+            s.iter += 1;
+            if (gn < mz.eps) s.done = 1;
+            else if (s.iter >= mz.maxiter) {
+                s.done = 1;
+                s.status = 2;
+            }
+        }
+        return;
+    }
+    // gdsq
+    if (fe < s.f_old) {
+        const double ms = -s.step;
+        double dot = 0.0, nn = 0.0;
+        for (int i = threadIdx.x; i < v.n; i += MT) {
+            const double gs = __dmul_rn(v.g[i], ms);
+            dot += gs * v.gt[i];
+            nn += gs * gs;
+        }
+        const double sum = block_reduce_sum(dot, red);
+        const double nrm = sqrt(block_reduce_sum(nn, red));
+        int gsmall = 1;
+        for (int i = threadIdx.x; i < v.n; i += MT) {
+            v.x[i] = v.xt[i];
+            v.g[i] = v.gt[i];
+            if (fabs(v.gt[i]) >= mz.gtol) gsmall = 0;
+        }
+        const int all_gsmall = block_all(gsmall, &flag);
+        double step = s.step;
+        const double aux = s.f_old - fe + sum;
+        if (aux <= 0.0) step *= mz.scale;
+        else step = 0.5 * nrm / aux;
+        int xsmall = 1;
+        const double xt = mz.xtol / step;
+        for (int i = threadIdx.x; i < v.n; i += MT)
+            if (fabs(v.g[i]) >= xt) xsmall = 0;
+        const int all_xsmall = block_all(xsmall, &flag);
+        if (threadIdx.x == 0) {
+            const double frel = s.f_old - fe;
+            s.f_old = fe;
+            s.f = fe;
+            s.step = step;
+            s.evals += 1;
+            if (all_gsmall) s.success |= 2;
+            if (frel < mz.ftolr) s.success |= 4;
+            if (all_xsmall) s.success |= 1;
+        }
+    } else {
+        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = v.x[i];
+        const double step = s.step / mz.scale;
+        int xsmall = 1;
+        const double xt = mz.xtol / step;
+        for (int i = threadIdx.x; i < v.n; i += MT)
+            if (fabs(v.g[i]) >= xt) xsmall = 0;
+        const int all_xsmall = block_all(xsmall, &flag);
+        if (threadIdx.x == 0) {
+            s.step = step;
+            s.evals += 1;
+            if (all_xsmall) s.success |= 1;
+        }
+    }
+}
+
+__global__ void k_count_active(const MinState *st, int npairs, int *count)
+{
+    int c = 0;
+    for (int p = threadIdx.x; p < npairs; p += blockDim.x) c += st[p].done ? 0 : 1;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (threadIdx.x == 0) *count = c;
+}
+
+template <class T>
+struct DArr {
+    T *p = nullptr;
+    ~DArr()
+    {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t n)
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        ck(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)), "cudaMalloc");
+    }
+    void upload(const std::vector<T> &h, cudaStream_t s)
+    {
+        alloc(h.size());
+        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
+    }
+};
+
+struct PairRun {
+    mgr_level_desc full{};
+    int size[3] = {1, 1, 1}, prev[3] = {0, 0, 0}, csize[3] = {1, 1, 1};
+    DArr<float> src, ref, src_n, ref_n, src_l, ref_l;
+    std::vector<double> params;
+    mgr_level *lvl = nullptr;
+    DArr<double> x, g, xt, gt, costs;
+    bool identity = false;   // both images of one value
+    bool in_pass = false;
+    double cost = 0.0;
+    int evals = 0;
+    ~PairRun()
+    {
+        if (lvl) mgr_level_destroy(lvl);
+    }
+};
+
+void ckm(mgr_status s)
+{
+    if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
+    if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
+}
+
+// Run the minimizer of every pair with in_pass set, in lock step, until all
+// have finished.  Steps are captured into a CUDA graph when use_graphs.
+void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_desc &mz, int dim, int tile[3],
+              bool use_graphs, cudaStream_t st)
+{
+    std::vector<int> members;
+    for (size_t i = 0; i < pairs.size(); ++i)
+        if (pairs[i]->in_pass) members.push_back(int(i));
+    const int np = int(members.size());
+    if (np == 0) return;
+    TraceScope tr_setup("batch: pass setup", st);
+    std::vector<EvalArgs> args(np);
+    std::vector<PairVec> vecs(np);
+    std::vector<MinState> states(np);
+    std::vector<int2> titems, gitems;
+    std::vector<int> nblocks(np);
+    size_t sm_warp = 0, sm_adj = 0;
+    int has_pen = 0;
+    for (int k = 0; k < np; ++k) {
+        PairRun &r = *pairs[members[k]];
+        const size_t n = r.params.size();
+        r.x.upload(r.params, st);
+        r.g.alloc(n);
+        r.xt.alloc(n);
+        r.gt.alloc(n);
+        r.costs.alloc(2);
+        EvalArgs a = r.lvl->args();
+        a.params = r.xt.p;
+        a.grad_total = r.gt.p;
+        a.grad_image = nullptr;
+        a.grad_penalty = nullptr;
+        a.costs = r.costs.p;
+        args[k] = a;
+        vecs[k] = PairVec{r.x.p, r.g.p, r.xt.p, r.gt.p, r.costs.p, int(n)};
+        MinState s{};
+        s.step = mz.step;
+        states[k] = s;
+        const int nt = a.ax[0].nt * a.ax[1].nt * (dim == 3 ? a.ax[2].nt : 1);
+        for (int t = 0; t < nt; ++t) titems.push_back(make_int2(k, t));
+        nblocks[k] = gather_blocks(a);
+        for (int b = 0; b < nblocks[k]; ++b) gitems.push_back(make_int2(k, b));
+        sm_warp = std::max(sm_warp, split_smem(a, 0));
+        sm_adj = std::max(sm_adj, split_smem(a, 1));
+        has_pen |= a.has_penalty;
+    }
+    DArr<EvalArgs> d_args;
+    DArr<PairVec> d_vecs;
+    DArr<MinState> d_states;
+    DArr<int2> d_titems, d_gitems;
+    DArr<int> d_nblocks, d_active, d_count;
+    d_args.upload(args, st);
+    d_vecs.upload(vecs, st);
+    d_states.upload(states, st);
+    d_titems.upload(titems, st);
+    d_gitems.upload(gitems, st);
+    d_nblocks.upload(nblocks, st);
+    d_active.alloc(np);
+    d_count.alloc(1);
+    ck(cudaMemsetAsync(d_active.p, 0, np * sizeof(int), st), "memset");
+
+    auto step = [&]() {
+        k_min_propose<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
+        if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
+                                d_active.p, sm_warp, 0, st))
+            throw std::invalid_argument("tile shape not compiled in");
+        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()), d_active.p,
+                           sm_adj, 1, st);
+        launch_gather_batch(dim, d_args.p, d_gitems.p, int(gitems.size()), d_active.p, d_nblocks.p, has_pen, st);
+        k_min_update<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
+        count_launch(2);
+    };
+    const int chunk = 8;
+    const int max_steps = 1 + (mz.maxiter + 2) * 64;   // bounded: GSL trials shrink the step geometrically
+    // kernel attributes are set outside the capture
+    prepare_split_batch(dim, tile[0], tile[1], tile[2], sm_warp, sm_adj);
+    cudaGraphExec_t exec = nullptr;
+    const unsigned kernels_per_chunk = unsigned(chunk) * 5 + 1;
+    tr_setup.stop();
+    if (use_graphs) {
+        TraceScope tr("batch: graph capture", st);
+        cudaGraph_t graph;
+        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture");
+        const unsigned long long before = mgr_kernel_launch_count();
+        for (int i = 0; i < chunk; ++i) step();
+        k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
+        count_launch();
+        ck(cudaStreamEndCapture(st, &graph), "end capture");
+        // launches recorded during capture run only when the graph runs
+        count_launch_adjust(before);
+        ck(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+    }
+    TraceScope tr_steps("batch: steps", st);
+    int steps = 0;
+    while (steps < max_steps) {
+        if (use_graphs) {
+            ck(cudaGraphLaunch(exec, st), "graph launch");
+            count_launch(kernels_per_chunk);
+        } else {
+            for (int i = 0; i < chunk; ++i) step();
+            k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
+            count_launch();
+        }
+        steps += chunk;
+        int active = 0;
+        ck(cudaMemcpyAsync(&active, d_count.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaStreamSynchronize(st), "batch sync");
+        if (active == 0) break;
+    }
+    tr_steps.stop();
+    TraceScope tr_back("batch: readback", st);
+    if (exec) cudaGraphExecDestroy(exec);
+    ck(cudaMemcpyAsync(states.data(), d_states.p, np * sizeof(MinState), cudaMemcpyDeviceToHost, st), "D2H");
+    for (int k = 0; k < np; ++k) {
+        PairRun &r = *pairs[members[k]];
+        ck(cudaMemcpyAsync(r.params.data(), r.x.p, r.params.size() * sizeof(double), cudaMemcpyDeviceToHost, st),
+           "D2H");
+    }
+    ck(cudaStreamSynchronize(st), "batch sync");
+    for (int k = 0; k < np; ++k) {
+        PairRun &r = *pairs[members[k]];
+        r.cost = states[k].f;
+        r.evals += states[k].evals;
+        round_params_to_float(r.params);
+    }
+}
+
+}  // namespace
+
+}  // namespace mgr
+
+using namespace mgr;
+
+namespace {
+
+// images_on_device: srcs/refs are device pointers of this device
+mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, const mgr_minimizer_desc *mz,
+                          const float *const *srcs, const float *const *refs, bool images_on_device, int device,
+                          int use_graphs, double *const *params_out, const size_t *max_params, int *csize_out,
+                          double *final_costs, int *evaluations)
+{
+    if (npairs < 1 || !descs || !mz || !srcs || !refs || !params_out || !max_params || !csize_out) {
+        set_last_error("mgr_register_batch: invalid argument");
+        return MGR_ERR_ARG;
+    }
+    try {
+        if (levels < 1) throw std::invalid_argument("levels must be >= 1");
+        const int dim = descs[0].dim;
+        if (dim != 2 && dim != 3) throw std::invalid_argument("dim must be 2 or 3");
+        if (mz->maxiter < 1) throw std::invalid_argument("maxiter must be >= 1");
+        for (int p = 0; p < npairs; ++p) {
+            if (!srcs[p] || !refs[p] || !params_out[p]) throw std::invalid_argument("null image or output pointer");
+            const mgr_level_desc &d = descs[p];
+            if (d.dim != dim) throw std::invalid_argument("all pairs of a batch must have the same dimension");
+            if (d.cost != descs[0].cost || d.has_penalty != descs[0].has_penalty)
+                throw std::invalid_argument("all pairs of a batch must use the same cost and penalty");
+            for (int k = 0; k < dim; ++k)
+                if (d.csize[k] != 0) throw std::invalid_argument("the batch derives the grids from the rate");
+        }
+        if (mz->kind != MGR_MIN_GSL_SD && mz->kind != MGR_MIN_GDSQ) throw std::invalid_argument("unknown minimizer");
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        cudaStream_t st;
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamDestroy(s); }
+        } guard{st};
+        int tile[3] = {32, 8, 8};
+        if (dim == 2) {
+            tile[1] = 16;
+            tile[2] = 1;
+        }
+        std::vector<std::unique_ptr<PairRun>> pairs;
+        TraceScope tr_in("batch: input+normalize", st);
+        for (int p = 0; p < npairs; ++p) {
+            std::unique_ptr<PairRun> r(new PairRun);
+            r->full = descs[p];
+            const size_t n = size_t(descs[p].size[0]) * descs[p].size[1] * (dim == 3 ? descs[p].size[2] : 1);
+            r->src_n.alloc(n);
+            r->ref_n.alloc(n);
+            const float *in_src = srcs[p], *in_ref = refs[p];
+            if (!images_on_device) {
+                r->src.alloc(n);
+                r->ref.alloc(n);
+                ck(cudaMemcpyAsync(r->src.p, srcs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+                ck(cudaMemcpyAsync(r->ref.p, refs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+                in_src = r->src.p;
+                in_ref = r->ref.p;
+            }
+            r->identity = !normalize_pair(in_src, in_ref, n, r->src_n.p, r->ref_n.p, st, nullptr, nullptr);
+            if (r->identity) {
+                for (int k = 0; k < 3; ++k)
+                    r->csize[k] = k < dim ? csize_from_rate(descs[p].size[k], descs[p].rate[k]) : 1;
+                r->params.assign(size_t(r->csize[0]) * r->csize[1] * r->csize[2] * dim, 0.0);
+            }
+            pairs.push_back(std::move(r));
+        }
+        tr_in.stop();
+        for (int shift = levels - 1; shift >= 0; --shift) {
+            TraceScope tr_scale("batch: upscale+scale filter", st);
+            for (auto &rp : pairs) {
+                PairRun &r = *rp;
+                r.in_pass = false;
+                if (r.identity) continue;
+                for (int k = 0; k < dim; ++k) r.size[k] = r.full.size[k] / (1 << shift);
+                if (shift == levels - 1) {
+                    for (int k = 0; k < 3; ++k) r.csize[k] = k < dim ? csize_from_rate(r.size[k], r.full.rate[k]) : 1;
+                    for (int k = 0; k < dim; ++k)
+                        if (r.csize[k] - 2 <= 1)
+                            throw std::invalid_argument("coefficient rate too large for the coarsest level");
+                    r.params.assign(size_t(r.csize[0]) * r.csize[1] * r.csize[2] * dim, 0.0);
+                } else {
+                    upscale_params(dim, r.prev, r.size, r.params);
+                }
+                const size_t n = size_t(r.size[0]) * r.size[1] * (dim == 3 ? r.size[2] : 1);
+                r.src_l.alloc(n);
+                r.ref_l.alloc(n);
+                scale_image(r.src_n.p, r.full.size, r.src_l.p, r.size, dim, st);
+                scale_image(r.ref_n.p, r.full.size, r.ref_l.p, r.size, dim, st);
+            }
+            tr_scale.stop();
+            for (int pass = 0; pass < 2; ++pass) {
+                TraceScope tr_lvl("batch: refine+level setup", st);
+                for (auto &rp : pairs) {
+                    PairRun &r = *rp;
+                    if (r.identity) continue;
+                    if (pass == 1) {
+                        int ncn[3] = {1, 1, 1};
+                        for (int k = 0; k < dim; ++k) ncn[k] = refine_csize(r.size[k], r.full.rate[k]);
+                        r.in_pass = refine_params(dim, r.csize, ncn, r.params);
+                        if (!r.in_pass) continue;
+                        for (int k = 0; k < 3; ++k) r.csize[k] = ncn[k];
+                    } else {
+                        r.in_pass = true;
+                    }
+                    if (r.lvl) {
+                        mgr_level_destroy(r.lvl);
+                        r.lvl = nullptr;
+                    }
+                    mgr_level_desc d = r.full;
+                    for (int k = 0; k < 3; ++k) {
+                        d.size[k] = k < dim ? r.size[k] : 1;
+                        d.csize[k] = k < dim ? r.csize[k] : 0;
+                    }
+                    ckm(mgr_level_create(&d, device, st, &r.lvl));
+                    ckm(mgr_level_set_path(r.lvl, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
+                    ckm(mgr_level_set_images_device(r.lvl, r.src_l.p, r.ref_l.p));
+                }
+                tr_lvl.stop();
+                run_pass(pairs, *mz, dim, tile, use_graphs != 0, st);
+            }
+            for (auto &rp : pairs)
+                for (int k = 0; k < 3; ++k) rp->prev[k] = rp->size[k];
+        }
+        trace_report("mgr_register_batch");
+        for (int p = 0; p < npairs; ++p) {
+            PairRun &r = *pairs[p];
+            if (r.params.size() > max_params[p]) throw std::invalid_argument("params_out too small");
+            std::copy(r.params.begin(), r.params.end(), params_out[p]);
+            for (int k = 0; k < 3; ++k) csize_out[p * 3 + k] = r.csize[k];
+            if (final_costs) final_costs[p] = r.cost;
+            if (evaluations) evaluations[p] = r.evals;
+        }
+        return MGR_OK;
+    } catch (const std::invalid_argument &e) {
+        set_last_error(e.what());
+        return MGR_ERR_ARG;
+    } catch (const std::bad_alloc &) {
+        set_last_error("allocation failed");
+        return MGR_ERR_OOM;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return MGR_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" mgr_status mgr_register_batch(int npairs, const mgr_level_desc *descs, int levels,
+                                         const mgr_minimizer_desc *mz, const float *const *srcs,
+                                         const float *const *refs, int device, int use_graphs,
+                                         double *const *params_out, const size_t *max_params, int *csize_out,
+                                         double *final_costs, int *evaluations)
+{
+    return register_batch(npairs, descs, levels, mz, srcs, refs, false, device, use_graphs, params_out, max_params,
+                          csize_out, final_costs, evaluations);
+}
+
+extern "C" mgr_status mgr_register_batch_device(int npairs, const mgr_level_desc *descs, int levels,
+                                                const mgr_minimizer_desc *mz, const float *const *d_srcs,
+                                                const float *const *d_refs, int device, int use_graphs,
+                                                double *const *params_out, const size_t *max_params,
+                                                int *csize_out, double *final_costs, int *evaluations)
+{
+    return register_batch(npairs, descs, levels, mz, d_srcs, d_refs, true, device, use_graphs, params_out,
+                          max_params, csize_out, final_costs, evaluations);
+}

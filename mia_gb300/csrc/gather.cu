@@ -23,8 +23,10 @@ constexpr int GC = 32;    // coefficients per block
 constexpr int NPART = 12; // per warp: penalty g[3], r[6]; image s[3]
 }  // namespace
 
+// block `blk` of the pair's `nblk` gather blocks
 template <int D>
-__global__ void __launch_bounds__(GT) k_gather_b(EvalArgs a, int with_gradient, int image_from_dense)
+__device__ __forceinline__ void gather_body(const EvalArgs &a, int with_gradient, int image_from_dense, int blk,
+                                            int nblk)
 {
     extern __shared__ float sm[];            // 3D: P table (9^3 x 6)
     __shared__ float part[GW][NPART][GC];
@@ -38,7 +40,7 @@ __global__ void __launch_bounds__(GT) k_gather_b(EvalArgs a, int with_gradient, 
         for (int e = tid; e < 9 * 9 * 9 * 6; e += GT) sm[e] = a.ptable[e];
         __syncthreads();
     }
-    const size_t i = size_t(blockIdx.x) * GC + lane;
+    const size_t i = size_t(blk) * GC + lane;
     const bool valid = i < ncoef;
     const int cx = valid ? int(i % ncx) : 0;
     const int cy = valid ? int((i / ncx) % ncy) : 0;
@@ -155,16 +157,16 @@ __global__ void __launch_bounds__(GT) k_gather_b(EvalArgs a, int with_gradient, 
         }
         pval = warp_sum(pval);
         if (lane == 0) {
-            a.pen_part[blockIdx.x] = pval;
+            a.pen_part[blk] = pval;
             __threadfence();
-            is_last = (atomicAdd(&a.counters[1], 1u) == gridDim.x - 1);
+            is_last = (atomicAdd(&a.counters[1], 1u) == unsigned(nblk - 1));
         }
     }
     __syncthreads();
     if (is_last) {
         __threadfence();
         double sv[1] = {0.0};
-        for (unsigned b = tid; b < gridDim.x; b += GT) sv[0] += ((volatile double *)a.pen_part)[b];
+        for (unsigned b = tid; b < unsigned(nblk); b += GT) sv[0] += ((volatile double *)a.pen_part)[b];
         block_sum<1>(sv, red);
         if (tid == 0) {
             double *sc = a.scalars;
@@ -180,6 +182,34 @@ __global__ void __launch_bounds__(GT) k_gather_b(EvalArgs a, int with_gradient, 
             a.counters[1] = 0;
         }
     }
+}
+
+template <int D>
+__global__ void __launch_bounds__(GT) k_gather_b(EvalArgs a, int with_gradient, int image_from_dense)
+{
+    gather_body<D>(a, with_gradient, image_from_dense, blockIdx.x, gridDim.x);
+}
+
+// batch: work list of (pair, block) items; finished pairs are skipped
+template <int D>
+__global__ void __launch_bounds__(GT) k_gather_batch(const EvalArgs *__restrict__ args, const int2 *__restrict__ items,
+                                                     const int *__restrict__ active, const int *__restrict__ nblocks)
+{
+    const int2 it = items[blockIdx.x];
+    if (!active[it.x]) return;
+    gather_body<D>(args[it.x], 1, 0, it.y, nblocks[it.x]);
+}
+
+void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int nitems, const int *active,
+                         const int *nblocks, int has_penalty, cudaStream_t st)
+{
+    if (dim == 3) {
+        const size_t sm = (has_penalty ? 9 * 9 * 9 * 6 : 0) * sizeof(float);
+        k_gather_batch<3><<<nitems, GT, sm, st>>>(args, items, active, nblocks);
+    } else {
+        k_gather_batch<2><<<nitems, GT, 0, st>>>(args, items, active, nblocks);
+    }
+    count_launch();
 }
 
 int gather_blocks(const EvalArgs &a)

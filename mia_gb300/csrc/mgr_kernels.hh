@@ -8,8 +8,11 @@
 
 namespace mgr {
 
-// launch accounting (mgr_kernel_launch_count)
+// launch accounting (mgr_kernel_launch_count); count_launch_adjust resets
+// the counter to `value` (launches recorded into a graph are counted when
+// the graph runs)
 void count_launch(unsigned n = 1);
+void count_launch_adjust(unsigned long long value);
 
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
 void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
@@ -61,6 +64,16 @@ void launch_gather_mode(const EvalArgs &a, int with_gradient, int dense, cudaStr
 int  gather_blocks(const EvalArgs &a);
 // tile shapes compiled into the split path
 bool tile_supported(int dim, int tx, int ty, int tz);
+
+// batched split path: one launch per phase over a work list of
+// (pair, tile) items (which = 0 warp, 1 adjoint) or (pair, block) items
+// (gather); pairs with active[pair] == 0 are skipped
+size_t split_smem(const EvalArgs &a, int which);
+void prepare_split_batch(int dim, int tx, int ty, int tz, size_t sm_warp, size_t sm_adj);
+bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, const int2 *items, int nitems,
+                        const int *active, size_t smem, int which, cudaStream_t st);
+void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int nitems, const int *active,
+                         const int *nblocks, int has_penalty, cudaStream_t st);
 
 // standalone pieces for tests and the plain path
 void launch_force(const EvalArgs &a, float *force, cudaStream_t st);       // force field from `warped`

@@ -13,6 +13,7 @@
 #include "mgr_kernels.hh"
 #include "pyramid.hh"
 #include "tables.hh"
+#include "trace.hh"
 
 namespace mgr {
 
@@ -69,7 +70,10 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
     ref_n.alloc(n_full);
     int evals = 0;
     double cost = 0.0;
-    if (!normalize_pair(d_src, d_ref, n_full, src_n.p, ref_n.p, st, nullptr, nullptr)) {
+    TraceScope tr_norm("pair: normalize", st);
+    const bool varied = normalize_pair(d_src, d_ref, n_full, src_n.p, ref_n.p, st, nullptr, nullptr);
+    tr_norm.stop();
+    if (!varied) {
         // both images of a single value: the identity transformation at full size
         for (int k = 0; k < 3; ++k) csize[k] = k < dim ? csize_from_rate(full.size[k], full.rate[k]) : 1;
         params.assign(size_t(csize[0]) * csize[1] * (dim == 3 ? csize[2] : 1) * dim, 0.0);
@@ -92,26 +96,32 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
             upscale_params(dim, prev_size, size, params);
         }
         const size_t n = size_t(size[0]) * size[1] * (dim == 3 ? size[2] : 1);
+        TraceScope tr_scale("pair: scale filter", st);
         src_l.alloc(n);
         ref_l.alloc(n);
         scale_image(src_n.p, full.size, src_l.p, size, dim, st);
         scale_image(ref_n.p, full.size, ref_l.p, size, dim, st);
+        tr_scale.stop();
         for (int pass = 0; pass < 2; ++pass) {
             mgr_level_desc d = full;
             for (int k = 0; k < 3; ++k) {
                 d.size[k] = size[k];
                 d.csize[k] = csize[k];
             }
+            TraceScope tr_lvl("pair: level setup", st);
             LevelHandle lv;
             ckm(mgr_level_create(&d, device, st, &lv.h));
             ckm(mgr_level_set_path(lv.h, path, 0, 0, 0));
             ckm(mgr_level_set_images_device(lv.h, src_l.p, ref_l.p));
+            tr_lvl.stop();
+            TraceScope tr_min("pair: minimizer", st);
             FDF fdf = [&](const std::vector<double> &x, std::vector<double> &g) {
                 double ci = 0, cp = 0;
                 ckm(mgr_level_evaluate(lv.h, x.data(), g.data(), nullptr, nullptr, &ci, &cp));
                 return ci + cp;
             };
             MinResult r = minimize(params, mz, fdf);
+            tr_min.stop();
             evals += r.evaluations;
             cost = r.f;
             round_params_to_float(params);
@@ -162,6 +172,7 @@ extern "C" mgr_status mgr_register(const mgr_level_desc *desc, int levels, const
             ck(cudaMemcpyAsync(d_src, src, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
             ck(cudaMemcpyAsync(d_ref, ref, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
             cost = register_pair_device(*desc, levels, *mz, d_src, d_ref, path, device, params, cs, evaluations, st);
+            trace_report("mgr_register");
         } catch (...) {
             cudaFree(d_src);
             cudaFree(d_ref);

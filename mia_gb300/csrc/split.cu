@@ -81,8 +81,9 @@ __device__ __forceinline__ void window_contract(int len, const int *start, const
 // ---------------------------------------------------------------------
 // warp
 // ---------------------------------------------------------------------
+// tile (bx, by, bz) of a pair with `ntiles` tiles, `tile` its linear index
 template <int D, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
+__device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int bz, int ntiles, int tile)
 {
     extern __shared__ float sm[];
     __shared__ double red[5 * (NT / 32)];
@@ -91,7 +92,6 @@ __global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
     __shared__ float4 fwx[TX], fwy[TY], fwz[TZ];
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = (D == 3) ? a.n[2] : 1;
-    const int bx = blockIdx.x, by = blockIdx.y, bz = (D == 3) ? blockIdx.z : 0;
     const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
     const int ex = min(TX, nx - x0), ey = min(TY, ny - y0), ez = min(TZ, nz - z0);
     const int FX = X.fc, FY = Y.fc, FZ = (D == 3) ? Z.fc : 1;
@@ -205,8 +205,6 @@ __global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
 #pragma unroll
     for (int k = 0; k < 5; ++k) dv[k] = acc[k];
     block_sum<5>(dv, red);
-    const int ntiles = gridDim.x * gridDim.y * gridDim.z;
-    const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) a.tile_sums[size_t(tile) * 5 + k] = dv[k];
@@ -225,7 +223,7 @@ __global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
 // gradient + force + adjoint
 // ---------------------------------------------------------------------
 template <int D, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
+__device__ __forceinline__ void adjoint_body(const EvalArgs &a, int bx, int by, int bz, int tile_index)
 {
     extern __shared__ float sm[];
     constexpr int HX = TX + 2, HY = TY + 2, HZ = (D == 3) ? TZ + 2 : 1;
@@ -234,14 +232,12 @@ __global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
     __shared__ float4 awx[TX], awy[TY], awz[TZ];
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = (D == 3) ? a.n[2] : 1;
-    const int bx = blockIdx.x, by = blockIdx.y, bz = (D == 3) ? blockIdx.z : 0;
     const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
     const int ex = min(TX, nx - x0), ey = min(TY, ny - y0), ez = min(TZ, nz - z0);
     const int AXc = X.ac, AYc = Y.ac, AZc = (D == 3) ? Z.ac : 1;
     const int ax0 = X.atile0[bx], ay0 = Y.atile0[by], az0 = (D == 3) ? Z.atile0[bz] : 0;
     const int tid = threadIdx.x;
-    const size_t tile = (size_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    float *part = a.partial + tile * a.slot;
+    float *part = a.partial + size_t(tile_index) * a.slot;
 
     float *Wh = sm;                          // [HZ][HY][HX]
     float *F = Wh + HZ * HY * HX;            // [D][TZ][TY][TXP]
@@ -335,6 +331,58 @@ __global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
             });
         }
     }
+}
+
+// ---------------------------------------------------------------------
+// kernels: one pair (grid = tiles) and a batch of pairs (grid = work list
+// of (pair, tile) items; pairs whose minimizer has finished are skipped)
+// ---------------------------------------------------------------------
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_warp_t(EvalArgs a)
+{
+    const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    warp_body<D, TX, TY, TZ>(a, blockIdx.x, blockIdx.y, D == 3 ? blockIdx.z : 0,
+                             gridDim.x * gridDim.y * gridDim.z, tile);
+}
+
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_adjoint_t(EvalArgs a)
+{
+    const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    adjoint_body<D, TX, TY, TZ>(a, blockIdx.x, blockIdx.y, D == 3 ? blockIdx.z : 0, tile);
+}
+
+__device__ __forceinline__ void decode_tile(const EvalArgs &a, int D, int t, int &bx, int &by, int &bz, int &nt)
+{
+    const int ntx = a.ax[0].nt, nty = a.ax[1].nt, ntz = D == 3 ? a.ax[2].nt : 1;
+    bx = t % ntx;
+    by = (t / ntx) % nty;
+    bz = t / (ntx * nty);
+    nt = ntx * nty * ntz;
+}
+
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_warp_batch(const EvalArgs *__restrict__ args, const int2 *__restrict__ items,
+                                                   const int *__restrict__ active)
+{
+    const int2 it = items[blockIdx.x];
+    if (!active[it.x]) return;
+    const EvalArgs &a = args[it.x];
+    int bx, by, bz, nt;
+    decode_tile(a, D, it.y, bx, by, bz, nt);
+    warp_body<D, TX, TY, TZ>(a, bx, by, bz, nt, it.y);
+}
+
+template <int D, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(NT) k_adjoint_batch(const EvalArgs *__restrict__ args,
+                                                      const int2 *__restrict__ items, const int *__restrict__ active)
+{
+    const int2 it = items[blockIdx.x];
+    if (!active[it.x]) return;
+    const EvalArgs &a = args[it.x];
+    int bx, by, bz, nt;
+    decode_tile(a, D, it.y, bx, by, bz, nt);
+    adjoint_body<D, TX, TY, TZ>(a, bx, by, bz, it.y);
 }
 
 // ---------------------------------------------------------------------
@@ -436,6 +484,81 @@ void launch_warp(const EvalArgs &a, cudaStream_t st)
 void launch_adjoint(const EvalArgs &a, cudaStream_t st)
 {
     dispatch(a, 1, st);
+}
+
+size_t split_smem(const EvalArgs &a, int which)
+{
+    return which == 0 ? warp_smem(a) : adjoint_smem(a);
+}
+
+template <int D, int TX, int TY, int TZ>
+static void launch_batch_tile(const EvalArgs *args, const int2 *items, int nitems, const int *active,
+                              size_t sm, int which, cudaStream_t st)
+{
+    if (which == 0)
+        k_warp_batch<D, TX, TY, TZ><<<nitems, NT, sm, st>>>(args, items, active);
+    else
+        k_adjoint_batch<D, TX, TY, TZ><<<nitems, NT, sm, st>>>(args, items, active);
+    count_launch();
+}
+
+template <int D, int TX, int TY, int TZ>
+static void prepare_batch_tile(size_t sm_warp, size_t sm_adj)
+{
+    cudaFuncSetAttribute(k_warp_batch<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_warp));
+    cudaFuncSetAttribute(k_adjoint_batch<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_adj));
+}
+
+void prepare_split_batch(int dim, int tx, int ty, int tz, size_t sm_warp, size_t sm_adj)
+{
+#define MGR_PTILE3(X_, Y_, Z_) \
+    if (dim == 3 && tx == X_ && ty == Y_ && tz == Z_) prepare_batch_tile<3, X_, Y_, Z_>(sm_warp, sm_adj);
+#define MGR_PTILE2(X_, Y_) \
+    if (dim == 2 && tx == X_ && ty == Y_) prepare_batch_tile<2, X_, Y_, 1>(sm_warp, sm_adj);
+    MGR_PTILE3(32, 8, 8)
+    MGR_PTILE3(32, 8, 4)
+    MGR_PTILE3(32, 4, 4)
+    MGR_PTILE3(64, 4, 4)
+    MGR_PTILE3(64, 8, 4)
+    MGR_PTILE3(32, 16, 4)
+    MGR_PTILE3(32, 16, 8)
+    MGR_PTILE2(32, 8)
+    MGR_PTILE2(32, 16)
+    MGR_PTILE2(64, 8)
+    MGR_PTILE2(64, 16)
+    MGR_PTILE2(32, 32)
+#undef MGR_PTILE3
+#undef MGR_PTILE2
+}
+
+bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, const int2 *items, int nitems,
+                        const int *active, size_t sm, int which, cudaStream_t st)
+{
+#define MGR_BTILE3(X_, Y_, Z_)                                                  \
+    if (dim == 3 && tx == X_ && ty == Y_ && tz == Z_) {                         \
+        launch_batch_tile<3, X_, Y_, Z_>(args, items, nitems, active, sm, which, st); \
+        return true;                                                            \
+    }
+#define MGR_BTILE2(X_, Y_)                                                      \
+    if (dim == 2 && tx == X_ && ty == Y_) {                                     \
+        launch_batch_tile<2, X_, Y_, 1>(args, items, nitems, active, sm, which, st); \
+        return true;                                                            \
+    }
+    MGR_BTILE3(32, 8, 8)
+    MGR_BTILE3(32, 8, 4)
+    MGR_BTILE3(32, 4, 4)
+    MGR_BTILE3(64, 4, 4)
+    MGR_BTILE3(64, 8, 4)
+    MGR_BTILE3(32, 16, 4)
+    MGR_BTILE3(32, 16, 8)
+    MGR_BTILE2(32, 8)
+    MGR_BTILE2(32, 16)
+    MGR_BTILE2(64, 8)
+    MGR_BTILE2(64, 16)
+    MGR_BTILE2(32, 32)
+#undef MGR_BTILE3
+#undef MGR_BTILE2
+    return false;
 }
 
 }  // namespace mgr

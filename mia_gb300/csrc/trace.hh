@@ -1,0 +1,43 @@
+// trace.hh — optional host-side phase timing of the registration drivers.
+// Enabled by the environment variable MGR_TRACE=1; each scope then waits
+// for its stream at exit and adds its wall-clock time to a named phase.
+// trace_report() prints the phases to stderr and clears them.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+
+namespace mgr {
+
+bool trace_enabled();
+void trace_add(const char *phase, double ms);
+void trace_report(const char *title);
+
+struct TraceScope {
+    const char *name;
+    cudaStream_t st;
+    bool on;
+    std::chrono::steady_clock::time_point t0;
+    TraceScope(const char *n, cudaStream_t s) : name(n), st(s), on(trace_enabled())
+    {
+        if (on) {
+            cudaStreamSynchronize(st);
+            t0 = std::chrono::steady_clock::now();
+        }
+    }
+    TraceScope(const TraceScope &) = delete;
+    TraceScope &operator=(const TraceScope &) = delete;
+    // record the phase now (the destructor then records nothing)
+    void stop()
+    {
+        if (on) {
+            cudaStreamSynchronize(st);
+            trace_add(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+            on = false;
+        }
+    }
+    ~TraceScope() { stop(); }
+};
+
+}  // namespace mgr

@@ -69,3 +69,54 @@ def normalize_pair(src, ref, device=0):
                                    ro.ctypes.data_as(_fp), ctypes.byref(m), ctypes.byref(sg), ctypes.byref(ok),
                                    int(device)))
     return bool(ok.value), so, ro, m.value, sg.value
+
+
+def _batch(shapes, sptrs, rptrs, on_device, rate, levels, mz, device, use_graphs, cost_kw):
+    n = len(shapes)
+    descs = (_lib.LevelDesc * n)()
+    for i, shp in enumerate(shapes):
+        descs[i] = level_desc(tuple(shp)[::-1], rate, **cost_kw)
+    sp = (ctypes.c_void_p * n)(*sptrs)
+    rp = (ctypes.c_void_p * n)(*rptrs)
+    # refine targets (size + rate - 1) / rate + 2 <= size + 2 coefficients per axis
+    maxp = [int(np.prod([d + 3 for d in shp])) * len(shp) for shp in shapes]
+    outs = [np.empty(m) for m in maxp]
+    op = (ctypes.POINTER(ctypes.c_double) * n)(*[o.ctypes.data_as(_dp) for o in outs])
+    mp = (ctypes.c_size_t * n)(*maxp)
+    cs = (ctypes.c_int * (3 * n))()
+    fc = (ctypes.c_double * n)()
+    ne = (ctypes.c_int * n)()
+    fn = lib().mgr_register_batch_device if on_device else lib().mgr_register_batch
+    check(fn(n, descs, int(levels), ctypes.byref(mz), sp, rp, int(device), int(bool(use_graphs)), op, mp, cs, fc, ne))
+    res = []
+    for i, shp in enumerate(shapes):
+        dim = len(shp)
+        c = tuple(cs[3 * i:3 * i + dim])
+        k = int(np.prod(c)) * dim
+        res.append((outs[i][:k].copy(), c, fc[i], ne[i]))
+    return res
+
+
+def register_batch(pairs, rate, levels, mz, device=0, use_graphs=True, **cost_kw):
+    """Register many (src, ref) host array pairs at once (sizes may differ;
+    one dimension, cost and penalty for all).  Returns a list of
+    (params, csize, final_cost, evaluations), one per pair."""
+    srcs = [np.ascontiguousarray(s, dtype=np.float32) for s, _ in pairs]
+    refs = [np.ascontiguousarray(r, dtype=np.float32) for _, r in pairs]
+    for s, r in zip(srcs, refs):
+        if s.shape != r.shape:
+            raise ValueError("source and reference of a pair differ in shape")
+    return _batch([s.shape for s in srcs], [s.ctypes.data for s in srcs], [r.ctypes.data for r in refs], False,
+                  rate, levels, mz, device, use_graphs, cost_kw)
+
+
+def register_batch_device(pairs, rate, levels, mz, device=0, use_graphs=True, **cost_kw):
+    """register_batch for pairs of contiguous float32 CUDA tensors (any
+    object with .shape, .data_ptr(), .is_contiguous() and .dtype)."""
+    for s, r in pairs:
+        if tuple(s.shape) != tuple(r.shape) or not (s.is_contiguous() and r.is_contiguous()):
+            raise ValueError("pairs must be contiguous tensors of equal shape")
+        if str(s.dtype) != "torch.float32" or str(r.dtype) != "torch.float32":
+            raise ValueError("pairs must be float32")
+    return _batch([tuple(s.shape) for s, _ in pairs], [s.data_ptr() for s, _ in pairs],
+                  [r.data_ptr() for _, r in pairs], True, rate, levels, mz, device, use_graphs, cost_kw)

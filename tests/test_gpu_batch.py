@@ -1,0 +1,109 @@
+"""Batched registration (mgr_register_batch): many pairs of uneven size in
+lock step with device-resident minimizers, against the oracle's per-pair
+registration and against the per-pair GPU driver."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+FINAL_COST_RTOL = 1e-4
+
+
+def _oracle_with_spread(mov, ref, rate, levels, mo, **kw):
+    """The oracle's registration and how far it moves when the moving image
+    is perturbed at float rounding level (relative 1e-7).  gdsq's step rule
+    divides by a difference of nearly equal numbers, so some trajectories
+    amplify rounding differences; agreement is then asserted within that
+    spread instead of the fixed tolerance."""
+    po, cso, fo, no = O.register(mov, ref, rate, levels, mo, **kw)
+    rng = np.random.default_rng(1)
+    m2 = (mov * (1 + 1e-7 * rng.standard_normal(mov.shape))).astype(np.float32)
+    p2, c2, f2, n2 = O.register(m2, ref, rate, levels, mo, **kw)
+    return po, cso, fo, abs(f2 - fo), np.linalg.norm(p2 - po)
+
+
+def _assert_close(pg, csg, fg, po, cso, fo, fspread, pspread):
+    assert csg == cso
+    assert abs(fg - fo) <= max(FINAL_COST_RTOL * abs(fo), 3 * fspread), (fg, fo, fspread)
+    assert np.linalg.norm(pg - po) <= max(1e-3 * np.linalg.norm(po), 3 * pspread)
+
+
+def _pair2d(seed, shape, rate=16.0):
+    from mia_gb300 import synth
+    ref = synth.blob_phantom(shape, 8, sigma=(4, 10), seed=seed)
+    lv = O.Level(shape[::-1], rate=rate)
+    lv.set_images(ref, ref)
+    mov = lv.warp(synth.spline_params(lv.nparams // 2, 2, 1.5, 3.0, seed=seed + 1))
+    return mov, ref
+
+
+def _pair3d(seed, shape, rate=8.0):
+    from mia_gb300 import synth
+    ref = synth.blob_phantom(shape, 10, sigma=(3, 8), seed=seed)
+    lv = O.Level(shape[::-1], rate=rate)
+    lv.set_images(ref, ref)
+    mov = lv.warp(synth.spline_params(lv.nparams // 3, 3, 1.5, 3.0, seed=seed + 1))
+    mov = (mov * synth.bias_field(shape, 0.1, seed=seed + 2)).astype(np.float32)
+    return mov, ref
+
+
+def test_batch_rejects_mixed_dimensions():
+    """argument checks run before any device call"""
+    from mia_gb300 import _lib
+    from mia_gb300 import registration as R
+    a = np.zeros((16, 16), np.float32)
+    b = np.zeros((8, 8, 8), np.float32)
+    with pytest.raises(_lib.MgrError) as e:
+        R.register_batch([(a, a), (b, b)], 4.0, 1, R.minimizer("gsl", maxiter=2))
+    assert e.value.status == _lib.MGR_ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["gsl", "gdsq"])
+def test_batch_2d_matches_oracle(kind):
+    from mia_gb300 import registration as R
+    shapes = [(80, 96), (64, 72), (96, 96), (72, 88)]
+    pairs = [_pair2d(31 + 7 * i, s) for i, s in enumerate(shapes)]
+    # a pair of constant images takes the identity shortcut
+    pairs.append((np.full((64, 64), 3.0, np.float32), np.full((64, 64), 3.0, np.float32)))
+    mg = R.minimizer(kind, maxiter=12, step=0.1)
+    res = R.register_batch(pairs, 16.0, 2, mg, cost="ssd", penalty_weight=10.0)
+    mo = O.minimizer(kind, maxiter=12, step=0.1)
+    for (mov, ref), (pg, csg, fg, ng) in zip(pairs[:-1], res[:-1]):
+        po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, 16.0, 2, mo, cost="ssd", penalty_weight=10.0)
+        _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
+    pg, csg, fg, ng = res[-1]
+    assert ng == 0 and fg == 0.0 and not np.any(pg)
+
+
+@pytest.mark.gpu
+def test_batch_3d_ncc_matches_oracle():
+    from mia_gb300 import registration as R
+    shapes = [(32, 36, 40), (24, 32, 32), (32, 32, 48)]
+    pairs = [_pair3d(41 + 5 * i, s) for i, s in enumerate(shapes)]
+    mg = R.minimizer("gdsq", maxiter=6, step=0.1)
+    res = R.register_batch(pairs, 8.0, 2, mg, cost="ncc", penalty_weight=5.0)
+    mo = O.minimizer("gdsq", maxiter=6, step=0.1)
+    for (mov, ref), (pg, csg, fg, ng) in zip(pairs, res):
+        po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, 8.0, 2, mo, cost="ncc", penalty_weight=5.0)
+        _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
+
+
+@pytest.mark.gpu
+def test_batch_graphs_match_stream_launches_and_per_pair_driver():
+    """graph replay and plain stream launches run the same kernels in the
+    same order: bit-identical results; the per-pair driver agrees within the
+    final-cost tolerance"""
+    from mia_gb300 import registration as R
+    shapes = [(64, 80), (96, 64), (80, 80)]
+    pairs = [_pair2d(51 + 3 * i, s) for i, s in enumerate(shapes)]
+    mg = R.minimizer("gsl", maxiter=20, step=0.1)
+    a = R.register_batch(pairs, 16.0, 2, mg, use_graphs=True, cost="ssd", penalty_weight=10.0)
+    b = R.register_batch(pairs, 16.0, 2, mg, use_graphs=False, cost="ssd", penalty_weight=10.0)
+    for (pa, ca, fa, na), (pb, cb, fb, nb) in zip(a, b):
+        assert ca == cb and fa == fb and na == nb
+        assert np.array_equal(pa, pb)
+    for (mov, ref), (pg, csg, fg, ng) in zip(pairs, a):
+        pp, csp, fp, npp = R.register_pair(mov, ref, 16.0, 2, mg, cost="ssd", penalty_weight=10.0)
+        assert csg == csp
+        assert abs(fg - fp) <= FINAL_COST_RTOL * abs(fp), (fg, fp)
