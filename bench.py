@@ -39,6 +39,19 @@ WORKLOADS = {
                                wclip=4.0, cost="ncc", penalty=5.0, bias=0.1, seed=3000),
 }
 
+# registration workloads (metric: registered pairs/s)
+BATCH_WORKLOADS = {
+    # 60-frame 2D perfusion series, frames of uneven size, all to frame 0
+    "series2d_60": dict(kind="series", npairs=60, rate=16.0, levels=2, cost="ssd", penalty=10.0, minimizer="gsl",
+                        maxiter=40, seed=4000),
+    # 16-pair 3D cohort of uneven size with bias fields
+    "cohort3d_16": dict(kind="cohort", npairs=16, rate=8.0, levels=3, cost="ncc", penalty=5.0, minimizer="gsl",
+                        maxiter=30, seed=5000),
+    # one 2D pair, 128x128, 1 level, 50 iterations
+    "single2d_128": dict(kind="single", npairs=1, rate=16.0, levels=1, cost="ssd", penalty=10.0, minimizer="gsl",
+                         maxiter=50, seed=1000),
+}
+
 
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -171,11 +184,153 @@ def cpu_baseline(w, mov, ref, params, seconds, threads):
     return N * n / dt / 1e6, n, dt, res
 
 
+def make_pairs(name, device):
+    """Host (moving, reference) pairs of a registration workload; the random
+    deformations are applied with this library's warp on `device`."""
+    import mia_gb300 as M
+    from mia_gb300 import synth
+    w = BATCH_WORKLOADS[name]
+
+    def warp_factory(dim):
+        def warp(img, rate, seed):
+            lv = M.Level(img.shape[::-1], rate=rate, device=device)
+            lv.set_images(img, img)
+            sig, clip = (1.5, 3.0) if dim == 2 else (2.0, 4.0)
+            p = synth.spline_params(lv.nparams // dim, dim, sig, clip, seed=seed)
+            out = lv.warp(p)
+            lv.close()
+            return out
+        return warp
+
+    if w["kind"] == "series":
+        pairs = synth.perfusion_series(w["npairs"], warp_factory(2), rate=w["rate"], seed=w["seed"])
+    elif w["kind"] == "cohort":
+        pairs = synth.cohort_pairs(w["npairs"], warp_factory(3), rate=w["rate"], seed=w["seed"])
+    else:
+        ref = synth.blob_phantom((128, 128), 12, sigma=(4.0, 12.0), seed=w["seed"])
+        pairs = [(warp_factory(2)(ref, w["rate"], w["seed"] + 1), ref)]
+    return w, pairs
+
+
+def oracle_pairs_per_s(w, pairs, seconds, threads):
+    """the oracle's registration of the pairs, one after the other with
+    `threads` threads per evaluation, until `seconds` have passed"""
+    from oracle import oracle as O
+    mo = O.minimizer(w["minimizer"], maxiter=w["maxiter"], step=0.1)
+    n = 0
+    t0 = time.perf_counter()
+    while n < len(pairs):
+        mov, ref = pairs[n]
+        O.register(mov, ref, w["rate"], w["levels"], mo, cost=w["cost"], penalty_weight=w["penalty"],
+                   threads=threads)
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def measure_batch(name, steps, warmup, device, cpu_seconds=0.0, clocks=None):
+    """Registered pairs/s of the batched path (device-resident images), end
+    to end from host arrays, and the per-pair GPU driver (plain and split
+    paths) on the same pairs."""
+    import torch
+    import mia_gb300 as M
+    from mia_gb300 import registration as R
+    w, pairs = make_pairs(name, device)
+    npairs = len(pairs)
+    mz = R.minimizer(w["minimizer"], maxiter=w["maxiter"], step=0.1)
+    kw = dict(cost=w["cost"], penalty_weight=w["penalty"])
+    dev = torch.device("cuda", device)
+    dpairs = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for a, b in pairs]
+    torch.cuda.synchronize()
+
+    def batch():
+        return R.register_batch_device(dpairs, w["rate"], w["levels"], mz, device=device, **kw)
+
+    for _ in range(warmup):
+        batch()
+    launches0 = M.lib().mgr_kernel_launch_count()
+    times = []
+    sampler = clocks if clocks is not None else ClockSampler(device)
+    with sampler:
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = batch()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    launches = (M.lib().mgr_kernel_launch_count() - launches0) // max(1, steps)
+    t_step = float(np.mean(times))
+    e2e_t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        res_h = R.register_batch(pairs, w["rate"], w["levels"], mz, device=device, **kw)
+        e2e_t.append(time.perf_counter() - t0)
+    t_e2e = float(np.mean(e2e_t))
+    per = {}
+    for path in ("plain", "split"):
+        t0 = time.perf_counter()
+        out = [R.register_pair(a, b, w["rate"], w["levels"], mz, path=path, device=device, **kw) for a, b in pairs]
+        per[path] = (npairs / (time.perf_counter() - t0), out)
+    plain_rate, plain_out = per["plain"]
+    rel = [abs(r[2] - o[2]) / max(abs(o[2]), 1e-300) for r, o in zip(res, plain_out)]
+    rel_split = [abs(r[2] - o[2]) / max(abs(o[2]), 1e-300) for r, o in zip(res, per["split"][1])]
+    h2d = int(sum(a.nbytes + b.nbytes for a, b in pairs))
+    d2h = int(sum(r[0].nbytes for r in res_h))
+    out = {
+        "value": npairs / t_step, "unit": "pairs/s", "ms_per_step": t_step * 1e3, "npairs": npairs,
+        "voxels": int(sum(a.size for a, _ in pairs)), "evaluations": int(sum(r[3] for r in res)),
+        "gpu_launches": int(launches),
+        "e2e": {"value": npairs / t_e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain_per_pair": {"value": plain_rate, "unit": "pairs/s", "path": "plain"},
+        "split_per_pair": {"value": per["split"][0], "unit": "pairs/s", "path": "split"},
+        "speedup_vs_plain_per_pair": {"device_resident": npairs / t_step / plain_rate,
+                                      "e2e": npairs / t_e2e / plain_rate},
+        "final_cost_rel_diff_vs_plain_per_pair": {"max": float(max(rel)), "median": float(np.median(rel))},
+        "final_cost_rel_diff_vs_split_per_pair": {"max": float(max(rel_split)),
+                                                  "median": float(np.median(rel_split))},
+        "config": {"workload": name, "pairs": npairs, "levels": w["levels"], "rate": w["rate"], "cost": w["cost"],
+                   "divcurl_weight": w["penalty"], "minimizer": "%s maxiter=%d step=0.1" % (w["minimizer"],
+                                                                                          w["maxiter"]),
+                   "sizes": sorted({"x".join(map(str, a.shape[::-1])) for a, _ in pairs})},
+    }
+    if cpu_seconds > 0:
+        threads = os.cpu_count() or 1
+        v, n, dt = oracle_pairs_per_s(w, pairs, cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
+                               "sample": "%d of the %d pairs registered in %.1f s" % (n, npairs, dt)}
+    return out
+
+
+def run_batch(args):
+    """one JSON line for a registration workload (pairs/s)"""
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    name = args.workload
+    clk = ClockSampler(local)
+    r = measure_batch(name, args.steps, args.warmup, local, 0.0 if args.no_cpu_baseline else args.cpu_seconds,
+                      clocks=clk)
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": ws * r["value"], "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
+    line["config"]["timing"] = "wall clock of the whole batched registration, device synchronised on both sides"
+    line["clocks"] = clk.summary()
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     name = args.workload
+    if name in BATCH_WORKLOADS:
+        return run_reference_batch(args)
     w = WORKLOADS[name]
     # inputs generated on the host only (the reference arm uses no GPU code)
     from mia_gb300 import synth
@@ -209,6 +364,51 @@ def run_reference(args):
                          "sample": "%d full evaluations of %s" % (args.steps, "x".join(map(str, size)))},
         "e2e": {"value": v, "unit": "Mvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line))
+    return 0
+
+
+def run_reference_batch(args):
+    """the oracle's registration on the host cores, pairs/s"""
+    w = BATCH_WORKLOADS[args.workload]
+    from mia_gb300 import synth
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+
+    def warp_factory(dim):
+        def warp(img, rate, seed):
+            lv = O.Level(img.shape[::-1], rate=rate, threads=threads)
+            lv.set_images(img, img)
+            sig, clip = (1.5, 3.0) if dim == 2 else (2.0, 4.0)
+            return lv.warp(synth.spline_params(lv.nparams // dim, dim, sig, clip, seed=seed))
+        return warp
+
+    if w["kind"] == "series":
+        pairs = synth.perfusion_series(w["npairs"], warp_factory(2), rate=w["rate"], seed=w["seed"])
+    elif w["kind"] == "cohort":
+        pairs = synth.cohort_pairs(w["npairs"], warp_factory(3), rate=w["rate"], seed=w["seed"])
+    else:
+        ref = synth.blob_phantom((128, 128), 12, sigma=(4.0, 12.0), seed=w["seed"])
+        pairs = [(warp_factory(2)(ref, w["rate"], w["seed"] + 1), ref)]
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        oracle_pairs_per_s(w, pairs[:1], 0.0, threads)
+    rates, counts = [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, n, dt = oracle_pairs_per_s(w, pairs, per_step, threads)
+        rates.append(v)
+        counts += n
+    dt = time.perf_counter() - t0
+    v = counts / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "pairs": len(pairs), "levels": w["levels"], "rate": w["rate"],
+                       "cost": w["cost"], "divcurl_weight": w["penalty"]},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": "%d pair registrations, %.1f s per step at most" % (counts, per_step)},
+            "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
@@ -329,6 +529,17 @@ def run_gpu(args):
             "grad_image_rel_l2": float(np.linalg.norm(gi - ogi) / np.linalg.norm(ogi)),
             "grad_penalty_rel_l2": float(np.linalg.norm(gp - ogp) / np.linalg.norm(ogp)),
             "against": "oracle, reference precision"}
+    if ws == 1 and not args.no_batched:
+        # the registration workloads (pairs/s): batched path against the
+        # per-pair GPU driver on the same pairs
+        lv.close()
+        line["batched"] = {}
+        for bname, cpu_s in (("series2d_60", 6.0), ("cohort3d_16", 10.0)):
+            bclk = ClockSampler(local)
+            r = measure_batch(bname, 2, 1, local, 0.0 if args.no_cpu_baseline else cpu_s, clocks=bclk)
+            r["clocks"] = bclk.summary()
+            r["steps"], r["warmup"] = 2, 1
+            line["batched"][bname] = r
     print(json.dumps(line))
     return 0
 
@@ -339,12 +550,15 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="3d_ssd_192x192x128", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="3d_ssd_192x192x128", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--no-batched", action="store_true", help="skip the registration summaries of the default line")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in BATCH_WORKLOADS:
+        return run_batch(args)
     return run_gpu(args)
 
 

@@ -2,6 +2,7 @@
 // memory, table upload and the evaluation pipelines.
 #include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -63,6 +64,24 @@ void trace_report(const char *title)
     std::fprintf(stderr, "[mgr trace] %s\n", title);
     for (auto &p : g_trace) std::fprintf(stderr, "  %-28s %10.3f ms  %6ld calls\n", p.name.c_str(), p.ms, p.n);
     g_trace.clear();
+}
+
+void configure_pool(int device)
+{
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    for (int d : done)
+        if (d == device) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        // freed blocks stay cached up to this size instead of returning to
+        // the device at every synchronisation
+        uint64_t keep = 8ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+    done.push_back(device);
 }
 
 static mgr_status fail(mgr_status s, const std::string &m)
@@ -144,23 +163,25 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         }
         L->device = device;
         ck(cudaSetDevice(device), "cudaSetDevice");
+        configure_pool(device);
         if (stream) {
             L->stream = static_cast<cudaStream_t>(stream);
         } else {
             ck(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate");
             L->own_stream = true;
         }
-        L->coef.alloc(L->N);
-        L->ref.alloc(L->N);
-        L->warped.alloc(L->N);
-        L->minmax.alloc(2);
-        L->mmpart.alloc(1024);
-        L->params.alloc(L->nparams);
-        L->grad_total.alloc(L->nparams);
-        L->scalars.alloc(SC_NSLOTS);
-        L->costs.alloc(2);
-        L->means.alloc(2);
-        L->counters.alloc(8);
+        L->coef.alloc(L->N, L->stream);
+        L->ref.alloc(L->N, L->stream);
+        L->warped.alloc(L->N, L->stream);
+        L->minmax.alloc(2, L->stream);
+        L->mmpart.alloc(1024, L->stream);
+        L->params.alloc(L->nparams, L->stream);
+        L->grad_total.alloc(L->nparams, L->stream);
+        L->scalars.alloc(SC_NSLOTS, L->stream);
+        L->costs.alloc(2, L->stream);
+        L->means.alloc(2, L->stream);
+        L->mpart.alloc(2 * 1024, L->stream);
+        L->counters.alloc(8, L->stream);
         ck(cudaMemsetAsync(L->counters.p, 0, 8 * sizeof(unsigned), L->stream), "memset");
         ck(cudaMemsetAsync(L->scalars.p, 0, SC_NSLOTS * sizeof(double), L->stream), "memset");
         L->build_tables();
@@ -170,15 +191,13 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
                 std::vector<float> P = build_penalty3(L->nc, range, d.pen_div, d.pen_curl);
                 L->ptable.upload(P, L->stream);
             } else {
-                std::vector<int> rp, col;
-                std::vector<float> val;
-                build_penalty2(L->nc, range, d.pen_div, d.pen_curl, rp, col, val);
-                L->pen_rowptr.upload(rp, L->stream);
-                L->pen_col.upload(col, L->stream);
-                L->pen_val.upload(val, L->stream);
+                const auto t = penalty2_cached(L->nc, range, d.pen_div, d.pen_curl);
+                L->pen_rowptr.upload(t->rowptr, L->stream);
+                L->pen_col.upload(t->col, L->stream);
+                L->pen_val.upload(t->val, L->stream);
             }
         }
-        ck(cudaStreamSynchronize(L->stream), "create sync");
+        check_launch("level create");
     });
     if (st == MGR_OK) *out = L.release();
     return st;
@@ -207,17 +226,34 @@ mgr_status mgr_level_csize(const mgr_level *lvl, int csize[3], size_t *nparams)
 
 }  // extern "C"
 
-// mean of a device image in double (NCC provisional centre)
-__global__ void k_mean(const float *__restrict__ img, size_t n, double *out)
+// means of the two images in double (NCC provisional centres): per-block
+// partial sums (blockIdx.y selects the image), then a fixed-order final sum
+__global__ void __launch_bounds__(256) k_mean_part(const float *__restrict__ a, const float *__restrict__ b, size_t n,
+                                                   double *part)
+{
+    __shared__ double red[8];
+    const float *img = blockIdx.y ? b : a;
+    double v[1] = {0.0};
+    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) v[0] += img[i];
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = v[0];
+}
+
+__global__ void __launch_bounds__(256) k_mean_final(const double *part, int nb, size_t n, double *out)
 {
     __shared__ double red[8];
     double v[1] = {0.0};
-    for (size_t i = threadIdx.x; i < n; i += blockDim.x) v[0] += img[i];
+    for (int i = threadIdx.x; i < nb; i += 256) v[0] += part[blockIdx.x * nb + i];
     block_sum<1>(v, red);
-    if (threadIdx.x == 0) *out = v[0] / double(n);
+    if (threadIdx.x == 0) out[blockIdx.x] = v[0] / double(n);
 }
 
-static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref)
+namespace mgr {
+
+// copy the images into the level, clamp bounds, centres and the prefilter,
+// all queued on the level's stream (the sources must stay valid until the
+// stream reaches them)
+void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref)
 {
     ck(cudaSetDevice(L->device), "cudaSetDevice");
     cudaStream_t st = L->stream;
@@ -226,17 +262,21 @@ static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref
         ck(cudaMemcpyAsync(L->ref.p, d_ref, L->N * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy ref");
     const int nb = int(std::min<size_t>(1024, (L->N + 255) / 256));
     launch_minmax(L->coef.p, L->N, L->mmpart.p, nb, L->counters.p + 4, L->minmax.p, st);
-    k_mean<<<1, 256, 0, st>>>(L->coef.p, L->N, L->means.p);
-    k_mean<<<1, 256, 0, st>>>(L->ref.p, L->N, L->means.p + 1);
+    k_mean_part<<<dim3(nb, 2), 256, 0, st>>>(L->coef.p, L->ref.p, L->N, L->mpart.p);
+    k_mean_final<<<2, 256, 0, st>>>(L->mpart.p, nb, L->N, L->means.p);
     count_launch(2);
     launch_prefilter(L->coef.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
     check_launch("set_images kernels");
-    double m[2];
-    ck(cudaMemcpyAsync(m, L->means.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "means");
-    ck(cudaStreamSynchronize(st), "set_images sync");
-    L->center_a = m[0];
-    L->center_b = m[1];
     L->images_set = true;
+}
+
+}  // namespace mgr
+
+static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref)
+{
+    level_set_images_async(L, d_src, d_ref);
+    // the caller may reuse its buffers once this returns
+    ck(cudaStreamSynchronize(L->stream), "set_images sync");
 }
 
 static void upload_params(mgr_level *L, const double *params)
@@ -258,11 +298,11 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
     if (L->path == MGR_PATH_PLAIN) {
         L->record(0);
         const size_t tsz = size_t(std::max(L->nc[2], 1)) * std::max(L->n[1], L->nc[1]) * L->n[0] * 3;
-        if (L->d.dim == 3) L->grid.alloc(L->N * 3);
-        L->force.alloc(L->N * L->d.dim);
-        L->tmp1.alloc(tsz);
-        L->tmp2.alloc(tsz);
-        L->grad_image.alloc(L->nparams);
+        if (L->d.dim == 3) L->grid.alloc(L->N * 3, L->stream);
+        L->force.alloc(L->N * L->d.dim, L->stream);
+        L->tmp1.alloc(tsz, L->stream);
+        L->tmp2.alloc(tsz, L->stream);
+        L->grad_image.alloc(L->nparams, L->stream);
         a.grad_image = L->grad_image.p;
         launch_plain_eval(a, L->grid.p, L->force.p, L->tmp1.p, L->tmp2.p, st);
         L->record(1);
@@ -289,7 +329,7 @@ mgr_status mgr_level_set_images(mgr_level *lvl, const float *src, const float *r
             if (!std::isfinite(src[i]) || !std::isfinite(ref[i]))
                 throw std::invalid_argument("images must be finite");
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
-        lvl->warped.alloc(lvl->N);
+        lvl->warped.alloc(lvl->N, lvl->stream);
         ck(cudaMemcpyAsync(lvl->warped.p, src, lvl->N * sizeof(float), cudaMemcpyHostToDevice, lvl->stream), "src");
         ck(cudaMemcpyAsync(lvl->ref.p, ref, lvl->N * sizeof(float), cudaMemcpyHostToDevice, lvl->stream), "ref");
         set_images_impl(lvl, lvl->warped.p, lvl->ref.p);
@@ -327,11 +367,11 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
         upload_params(lvl, params);
         EvalArgs a = lvl->args();
         if (grad_image && lvl->path != MGR_PATH_PLAIN) {
-            lvl->grad_image.alloc(lvl->nparams);
+            lvl->grad_image.alloc(lvl->nparams, lvl->stream);
             a.grad_image = lvl->grad_image.p;
         }
         if (grad_penalty) {
-            lvl->grad_penalty.alloc(lvl->nparams);
+            lvl->grad_penalty.alloc(lvl->nparams, lvl->stream);
             a.grad_penalty = lvl->grad_penalty.p;
         }
         run_image_term(lvl, a, true);
@@ -393,7 +433,7 @@ mgr_status mgr_level_force(mgr_level *lvl, const double *params, float *force, d
         upload_params(lvl, params);
         EvalArgs a = lvl->args();
         launch_warp(a, lvl->stream);
-        lvl->force.alloc(lvl->N * lvl->d.dim);
+        lvl->force.alloc(lvl->N * lvl->d.dim, lvl->stream);
         launch_force(a, lvl->force.p, lvl->stream);
         check_launch("force kernels");
         ck(cudaMemcpyAsync(force, lvl->force.p, lvl->N * lvl->d.dim * sizeof(float), cudaMemcpyDeviceToHost,
@@ -412,11 +452,11 @@ mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad)
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
         cudaStream_t st = lvl->stream;
         const int D = lvl->d.dim;
-        lvl->force.alloc(lvl->N * D);
+        lvl->force.alloc(lvl->N * D, lvl->stream);
         const size_t tsz = size_t(std::max(lvl->nc[2], 1)) * std::max(lvl->n[1], lvl->nc[1]) * lvl->n[0] * 3;
-        lvl->tmp1.alloc(tsz);
-        lvl->tmp2.alloc(tsz);
-        lvl->grad_image.alloc(lvl->nparams);
+        lvl->tmp1.alloc(tsz, lvl->stream);
+        lvl->tmp2.alloc(tsz, lvl->stream);
+        lvl->grad_image.alloc(lvl->nparams, lvl->stream);
         ck(cudaMemcpyAsync(lvl->force.p, force, lvl->N * D * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
         EvalArgs a = lvl->args();
         a.cost_weight = 1.0;

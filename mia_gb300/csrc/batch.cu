@@ -267,33 +267,13 @@ __global__ void k_count_active(const MinState *st, int npairs, int *count)
     if (threadIdx.x == 0) *count = c;
 }
 
-template <class T>
-struct DArr {
-    T *p = nullptr;
-    ~DArr()
-    {
-        if (p) cudaFree(p);
-    }
-    void alloc(size_t n)
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        ck(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)), "cudaMalloc");
-    }
-    void upload(const std::vector<T> &h, cudaStream_t s)
-    {
-        alloc(h.size());
-        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
-    }
-};
-
 struct PairRun {
     mgr_level_desc full{};
     int size[3] = {1, 1, 1}, prev[3] = {0, 0, 0}, csize[3] = {1, 1, 1};
-    DArr<float> src, ref, src_n, ref_n, src_l, ref_l;
+    DevBuf<float> src, ref, src_n, ref_n, src_l, ref_l;
     std::vector<double> params;
     mgr_level *lvl = nullptr;
-    DArr<double> x, g, xt, gt, costs;
+    DevBuf<double> x, g, xt, gt, costs;
     bool identity = false;   // both images of one value
     bool in_pass = false;
     double cost = 0.0;
@@ -332,10 +312,10 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         PairRun &r = *pairs[members[k]];
         const size_t n = r.params.size();
         r.x.upload(r.params, st);
-        r.g.alloc(n);
-        r.xt.alloc(n);
-        r.gt.alloc(n);
-        r.costs.alloc(2);
+        r.g.alloc(n, st);
+        r.xt.alloc(n, st);
+        r.gt.alloc(n, st);
+        r.costs.alloc(2, st);
         EvalArgs a = r.lvl->args();
         a.params = r.xt.p;
         a.grad_total = r.gt.p;
@@ -355,19 +335,19 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         sm_adj = std::max(sm_adj, split_smem(a, 1));
         has_pen |= a.has_penalty;
     }
-    DArr<EvalArgs> d_args;
-    DArr<PairVec> d_vecs;
-    DArr<MinState> d_states;
-    DArr<int2> d_titems, d_gitems;
-    DArr<int> d_nblocks, d_active, d_count;
+    DevBuf<EvalArgs> d_args;
+    DevBuf<PairVec> d_vecs;
+    DevBuf<MinState> d_states;
+    DevBuf<int2> d_titems, d_gitems;
+    DevBuf<int> d_nblocks, d_active, d_count;
     d_args.upload(args, st);
     d_vecs.upload(vecs, st);
     d_states.upload(states, st);
     d_titems.upload(titems, st);
     d_gitems.upload(gitems, st);
     d_nblocks.upload(nblocks, st);
-    d_active.alloc(np);
-    d_count.alloc(1);
+    d_active.alloc(np, st);
+    d_count.alloc(1, st);
     ck(cudaMemsetAsync(d_active.p, 0, np * sizeof(int), st), "memset");
 
     auto step = [&]() {
@@ -471,6 +451,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         }
         if (mz->kind != MGR_MIN_GSL_SD && mz->kind != MGR_MIN_GDSQ) throw std::invalid_argument("unknown minimizer");
         ck(cudaSetDevice(device), "cudaSetDevice");
+        configure_pool(device);
         cudaStream_t st;
         ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
         struct StreamGuard {
@@ -488,12 +469,12 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             std::unique_ptr<PairRun> r(new PairRun);
             r->full = descs[p];
             const size_t n = size_t(descs[p].size[0]) * descs[p].size[1] * (dim == 3 ? descs[p].size[2] : 1);
-            r->src_n.alloc(n);
-            r->ref_n.alloc(n);
+            r->src_n.alloc(n, st);
+            r->ref_n.alloc(n, st);
             const float *in_src = srcs[p], *in_ref = refs[p];
             if (!images_on_device) {
-                r->src.alloc(n);
-                r->ref.alloc(n);
+                r->src.alloc(n, st);
+                r->ref.alloc(n, st);
                 ck(cudaMemcpyAsync(r->src.p, srcs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
                 ck(cudaMemcpyAsync(r->ref.p, refs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
                 in_src = r->src.p;
@@ -525,8 +506,8 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                     upscale_params(dim, r.prev, r.size, r.params);
                 }
                 const size_t n = size_t(r.size[0]) * r.size[1] * (dim == 3 ? r.size[2] : 1);
-                r.src_l.alloc(n);
-                r.ref_l.alloc(n);
+                r.src_l.alloc(n, st);
+                r.ref_l.alloc(n, st);
                 scale_image(r.src_n.p, r.full.size, r.src_l.p, r.size, dim, st);
                 scale_image(r.ref_n.p, r.full.size, r.ref_l.p, r.size, dim, st);
             }
@@ -556,7 +537,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                     }
                     ckm(mgr_level_create(&d, device, st, &r.lvl));
                     ckm(mgr_level_set_path(r.lvl, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
-                    ckm(mgr_level_set_images_device(r.lvl, r.src_l.p, r.ref_l.p));
+                    level_set_images_async(r.lvl, r.src_l.p, r.ref_l.p);
                 }
                 tr_lvl.stop();
                 run_pass(pairs, *mz, dim, tile, use_graphs != 0, st);

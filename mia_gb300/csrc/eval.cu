@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) k_warp_plain(EvalArgs a, const float *gri
             const float d = wv - b;
             acc[0] = d * d;
         } else {
-            const float da = wv - float(a.center_a), db = b - float(a.center_b);
+            const float da = wv - float(a.centers[0]), db = b - float(a.centers[1]);
             acc[0] = da; acc[1] = db; acc[2] = da * da; acc[3] = db * db; acc[4] = da * db;
         }
     }

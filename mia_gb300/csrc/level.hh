@@ -31,32 +31,42 @@ inline void ck(cudaError_t e, const char *what)
     }
 }
 
+// Keep freed stream-ordered allocations of `device` cached in its default
+// memory pool (up to a bound) so that repeated level setup does not map and
+// unmap device memory.
+void configure_pool(int device);
+
+// Device buffer in stream-ordered memory: allocated on and freed on the
+// stream given to alloc(), which must outlive the buffer.  Growing keeps the
+// old contents only when the old allocation is large enough.
 template <class T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t st = nullptr;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, st);
         p = nullptr;
         n = 0;
     }
-    void alloc(size_t count)
+    void alloc(size_t count, cudaStream_t s)
     {
         if (count <= n && p) return;
         release();
         if (count == 0) return;
-        ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        ck(cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), s), "cudaMallocAsync");
+        st = s;
         n = count;
     }
-    void upload(const std::vector<T> &h, cudaStream_t st)
+    void upload(const std::vector<T> &h, cudaStream_t s)
     {
-        alloc(h.size());
-        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+        alloc(h.size(), s);
+        if (!h.empty()) ck(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
     }
 };
 
@@ -112,12 +122,11 @@ struct mgr_level {
     AxisDev ax[3];
     DevBuf<float> coef, ref, warped, minmax, partial, ptable, pen_val;
     DevBuf<float2> mmpart;
-    DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means;
+    DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means, mpart;
     DevBuf<unsigned int> counters;
     DevBuf<int> pen_rowptr, pen_col;
     DevBuf<float> grid, force, tmp1, tmp2;   // plain path and standalone force/translate
     int slot = 0;
-    double center_a = 0.0, center_b = 0.0;
     bool images_set = false;
     bool tables_valid = false;
     bool timing = false;
@@ -150,8 +159,7 @@ struct mgr_level {
         a.cost = d.cost;
         a.ssd_norm = d.ssd_norm;
         a.cost_weight = d.cost_weight;
-        a.center_a = center_a;
-        a.center_b = center_b;
+        a.centers = means.p;
         a.partial = partial.p;
         a.slot = slot;
         a.tile_sums = tile_sums.p;
@@ -182,11 +190,15 @@ struct mgr_level {
         }
         const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
         slot = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
-        partial.alloc(size_t(ntiles) * slot);
+        partial.alloc(size_t(ntiles) * slot, stream);
         const size_t plain_blocks = (N + 255) / 256;
-        tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5);
-        pen_part.alloc(size_t(gather_blocks(args())) + 1);
+        tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5, stream);
+        pen_part.alloc(size_t(gather_blocks(args())) + 1, stream);
         tables_valid = true;
     }
 };
 
+namespace mgr {
+// mgr_level_set_images_device without the final stream synchronisation
+void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref);
+}  // namespace mgr

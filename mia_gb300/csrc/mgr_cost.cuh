@@ -25,7 +25,7 @@ __device__ __forceinline__ void finalise_cost(const EvalArgs &a, const double s[
     }
     const double n = double(N);
     const double sa = s[0], sb = s[1], saa = s[2], sbb = s[3], sab = s[4];
-    const double ma = a.center_a + sa / n, mb = a.center_b + sb / n;
+    const double ma = a.centers[0] + sa / n, mb = a.centers[1] + sb / n;
     const double s2a = saa - sa * sa / n;
     const double s2b = sbb - sb * sb / n;
     const double cab = sab - sa * sb / n;

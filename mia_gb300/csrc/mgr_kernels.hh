@@ -32,7 +32,8 @@ struct EvalArgs {
     int cost;              // MGR_COST_SSD / NCC
     int ssd_norm;
     double cost_weight;
-    double center_a, center_b;  // NCC provisional centres (reduce cancellation)
+    const double *centers; // device {mean src, mean ref}: NCC provisional centres
+                           // (sums are taken around them to reduce cancellation)
     // tile partials and reductions
     float *partial;        // per tile adjoint footprint partials
     int slot;              // floats per tile slot

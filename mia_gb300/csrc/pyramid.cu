@@ -195,12 +195,14 @@ template <class TI, class TO>
 void scale_axis(const TI *in, TO *out, const AxisPlan &p, int n_in, int n_out, int nlines, size_t ils, size_t ies,
                 size_t ols, size_t oes, int lpp, size_t ips, size_t ops, cudaStream_t st)
 {
+    // stream-ordered temporaries; the plan's host vectors may go away once
+    // the (pageable) copies have been issued
     double *d_mask = nullptr;
     int4 *d_idx = nullptr;
     Wt4 *d_wts = nullptr;
-    ck(cudaMalloc(&d_mask, p.mask.size() * sizeof(double)), "cudaMalloc");
-    ck(cudaMalloc(&d_idx, p.idx.size() * sizeof(int4)), "cudaMalloc");
-    ck(cudaMalloc(&d_wts, p.wts.size() * sizeof(Wt4)), "cudaMalloc");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_mask), p.mask.size() * sizeof(double), st), "cudaMallocAsync");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_idx), p.idx.size() * sizeof(int4), st), "cudaMallocAsync");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_wts), p.wts.size() * sizeof(Wt4), st), "cudaMallocAsync");
     ck(cudaMemcpyAsync(d_mask, p.mask.data(), p.mask.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
     ck(cudaMemcpyAsync(d_idx, p.idx.data(), p.idx.size() * sizeof(int4), cudaMemcpyHostToDevice, st), "H2D");
     ck(cudaMemcpyAsync(d_wts, p.wts.data(), p.wts.size() * sizeof(Wt4), cudaMemcpyHostToDevice, st), "H2D");
@@ -212,10 +214,9 @@ void scale_axis(const TI *in, TO *out, const AxisPlan &p, int n_in, int n_out, i
                                                                   lpp, ips, ops, p.gw, d_mask, d_idx, d_wts);
     count_launch();
     ck(cudaGetLastError(), "scale kernel");
-    ck(cudaStreamSynchronize(st), "scale sync");
-    cudaFree(d_mask);
-    cudaFree(d_idx);
-    cudaFree(d_wts);
+    cudaFreeAsync(d_mask, st);
+    cudaFreeAsync(d_idx, st);
+    cudaFreeAsync(d_wts, st);
 }
 
 }  // namespace
@@ -232,13 +233,13 @@ bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_s
 {
     const int nb = int(std::min<size_t>(512, (n + 255) / 256));
     double *d_part = nullptr;
-    ck(cudaMalloc(&d_part, size_t(nb) * 2 * sizeof(double)), "cudaMalloc");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), size_t(nb) * 2 * sizeof(double), st), "cudaMallocAsync");
     k_pair_sums<<<nb, 256, 0, st>>>(d_src, d_ref, n, d_part);
     count_launch();
     std::vector<double> part(size_t(nb) * 2);
     ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    cudaFreeAsync(d_part, st);
     ck(cudaStreamSynchronize(st), "sync");
-    cudaFree(d_part);
     double sum = 0.0, sum2 = 0.0;
     for (int b = 0; b < nb; ++b) {
         sum += part[2 * b];
@@ -276,7 +277,7 @@ void scale_image(const float *d_in, const int in_size[3], float *d_out, const in
             throw std::invalid_argument("scale: only downscaling to sizes >= 2 is supported");
     // x: float -> double, lines = rows (y, z)
     double *t1 = nullptr, *t2 = nullptr;
-    ck(cudaMalloc(&t1, size_t(mx) * ny * nz * sizeof(double)), "cudaMalloc");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&t1), size_t(mx) * ny * nz * sizeof(double), st), "cudaMallocAsync");
     const AxisPlan px = plan_axis(nx, mx);
     const AxisPlan py = plan_axis(ny, my);
     // C1DScalar copies when the size does not change on an axis
@@ -287,17 +288,17 @@ void scale_image(const float *d_in, const int in_size[3], float *d_out, const in
     if (dim == 2) {
         // y: double -> float, lines = columns x, stride mx
         scale_axis(t1, d_out, py, ny, my, mx, 1, size_t(mx), 1, size_t(mx), mx, 0, 0, st);
-        cudaFree(t1);
+        cudaFreeAsync(t1, st);
         return;
     }
-    ck(cudaMalloc(&t2, size_t(mx) * my * nz * sizeof(double)), "cudaMalloc");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&t2), size_t(mx) * my * nz * sizeof(double), st), "cudaMallocAsync");
     // y: lines = (x, z): per plane z, mx lines of stride 1, element stride mx
     scale_axis(t1, t2, py, ny, my, mx * nz, 1, size_t(mx), 1, size_t(mx), mx, size_t(mx) * ny, size_t(mx) * my, st);
     // z: lines = (x, y): mx*my lines, element stride mx*my
     const AxisPlan pz = plan_axis(nz, mz);
     scale_axis(t2, d_out, pz, nz, mz, mx * my, 1, size_t(mx) * my, 1, size_t(mx) * my, mx * my, 0, 0, st);
-    cudaFree(t1);
-    cudaFree(t2);
+    cudaFreeAsync(t1, st);
+    cudaFreeAsync(t2, st);
 }
 
 }  // namespace mgr

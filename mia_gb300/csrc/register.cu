@@ -10,7 +10,7 @@
 
 #include "../../include/mgr.h"
 #include "driver.hh"
-#include "mgr_kernels.hh"
+#include "level.hh"
 #include "pyramid.hh"
 #include "tables.hh"
 #include "trace.hh"
@@ -21,30 +21,11 @@ void set_last_error(const std::string &msg);
 
 namespace {
 
-void ck(cudaError_t e, const char *what)
-{
-    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
-}
-
 void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
     if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
 }
-
-struct DevImage {
-    float *p = nullptr;
-    ~DevImage()
-    {
-        if (p) cudaFree(p);
-    }
-    void alloc(size_t n)
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        ck(cudaMalloc(&p, n * sizeof(float)), "cudaMalloc");
-    }
-};
 
 struct LevelHandle {
     mgr_level *h = nullptr;
@@ -65,9 +46,9 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
     const int dim = full.dim;
     const int nz = dim == 3 ? full.size[2] : 1;
     const size_t n_full = size_t(full.size[0]) * full.size[1] * nz;
-    DevImage src_n, ref_n, src_l, ref_l;
-    src_n.alloc(n_full);
-    ref_n.alloc(n_full);
+    DevBuf<float> src_n, ref_n, src_l, ref_l;
+    src_n.alloc(n_full, st);
+    ref_n.alloc(n_full, st);
     int evals = 0;
     double cost = 0.0;
     TraceScope tr_norm("pair: normalize", st);
@@ -97,8 +78,8 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
         }
         const size_t n = size_t(size[0]) * size[1] * (dim == 3 ? size[2] : 1);
         TraceScope tr_scale("pair: scale filter", st);
-        src_l.alloc(n);
-        ref_l.alloc(n);
+        src_l.alloc(n, st);
+        ref_l.alloc(n, st);
         scale_image(src_n.p, full.size, src_l.p, size, dim, st);
         scale_image(ref_n.p, full.size, ref_l.p, size, dim, st);
         tr_scale.stop();
@@ -112,7 +93,7 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
             LevelHandle lv;
             ckm(mgr_level_create(&d, device, st, &lv.h));
             ckm(mgr_level_set_path(lv.h, path, 0, 0, 0));
-            ckm(mgr_level_set_images_device(lv.h, src_l.p, ref_l.p));
+            level_set_images_async(lv.h, src_l.p, ref_l.p);
             tr_lvl.stop();
             TraceScope tr_min("pair: minimizer", st);
             FDF fdf = [&](const std::vector<double> &x, std::vector<double> &g) {
@@ -158,30 +139,32 @@ extern "C" mgr_status mgr_register(const mgr_level_desc *desc, int levels, const
         if (mz->kind != MGR_MIN_GSL_SD && mz->kind != MGR_MIN_GDSQ) throw std::invalid_argument("unknown minimizer");
         if (mz->maxiter < 1) throw std::invalid_argument("maxiter must be >= 1");
         ck(cudaSetDevice(device), "cudaSetDevice");
+        configure_pool(device);
         cudaStream_t st;
         ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard()
+            {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+        } guard{st};
         const int dim = desc->dim;
         const size_t n = size_t(desc->size[0]) * desc->size[1] * (dim == 3 ? desc->size[2] : 1);
-        float *d_src = nullptr, *d_ref = nullptr;
-        ck(cudaMalloc(&d_src, n * sizeof(float)), "cudaMalloc");
-        ck(cudaMalloc(&d_ref, n * sizeof(float)), "cudaMalloc");
         std::vector<double> params;
         int cs[3] = {1, 1, 1};
         double cost = 0.0;
-        try {
-            ck(cudaMemcpyAsync(d_src, src, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
-            ck(cudaMemcpyAsync(d_ref, ref, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
-            cost = register_pair_device(*desc, levels, *mz, d_src, d_ref, path, device, params, cs, evaluations, st);
+        {
+            DevBuf<float> d_src, d_ref;
+            d_src.alloc(n, st);
+            d_ref.alloc(n, st);
+            ck(cudaMemcpyAsync(d_src.p, src, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+            ck(cudaMemcpyAsync(d_ref.p, ref, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
+            cost = register_pair_device(*desc, levels, *mz, d_src.p, d_ref.p, path, device, params, cs, evaluations,
+                                        st);
             trace_report("mgr_register");
-        } catch (...) {
-            cudaFree(d_src);
-            cudaFree(d_ref);
-            cudaStreamDestroy(st);
-            throw;
         }
-        cudaFree(d_src);
-        cudaFree(d_ref);
-        cudaStreamDestroy(st);
         if (params.size() > max_params) throw std::invalid_argument("params_out too small");
         std::copy(params.begin(), params.end(), params_out);
         for (int k = 0; k < 3; ++k) csize_out[k] = cs[k];

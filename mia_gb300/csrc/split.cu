@@ -167,7 +167,7 @@ __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int
     // x stage, tricubic sample, warped image, sums
     float acc[5] = {0, 0, 0, 0, 0};
     const float mn = a.minmax[0], mxv = a.minmax[1];
-    const float ca = float(a.center_a), cb = float(a.center_b);
+    const float ca = float(a.centers[0]), cb = float(a.centers[1]);
     constexpr int NV = TX * TY * TZ;
     for (int v = tid; v < NV; v += NT) {
         const int xx = v % TX, yy = (v / TX) % TY, zz = v / (TX * TY);

@@ -11,7 +11,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <memory>
+#include <mutex>
 #include <stdexcept>
 
 namespace mgr {
@@ -327,6 +330,27 @@ void build_penalty2(const int csize[2], const float range[2], double wd, double 
         val[e * 4 + 2] = cells[e].v12;
         val[e * 4 + 3] = 0.0f;
     }
+}
+
+std::shared_ptr<const Penalty2Table> penalty2_cached(const int csize[2], const float range[2], double wd, double wr)
+{
+    struct Entry {
+        int c0, c1;
+        float r0, r1;
+        double wd, wr;
+        std::shared_ptr<const Penalty2Table> t;
+    };
+    static std::mutex mu;
+    static std::deque<Entry> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Entry &e : cache)
+        if (e.c0 == csize[0] && e.c1 == csize[1] && e.r0 == range[0] && e.r1 == range[1] && e.wd == wd && e.wr == wr)
+            return e.t;
+    std::shared_ptr<Penalty2Table> t(new Penalty2Table);
+    build_penalty2(csize, range, wd, wr, t->rowptr, t->col, t->val);
+    if (cache.size() >= 64) cache.pop_front();   // bounded: the oldest table goes first
+    cache.push_back(Entry{csize[0], csize[1], range[0], range[1], wd, wr, t});
+    return t;
 }
 
 }  // namespace mgr

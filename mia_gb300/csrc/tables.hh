@@ -1,6 +1,7 @@
 // tables.hh — host-side per-level tables (see tables.cc).
 #pragma once
 
+#include <memory>
 #include <vector>
 
 namespace mgr {
@@ -23,5 +24,13 @@ void build_axis(AxisHost &ax, int n, int nc, int tile);
 std::vector<float> build_penalty3(const int csize[3], const float range[3], double wdiv, double wrot);
 void build_penalty2(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
                     std::vector<int> &col, std::vector<float> &val);
+
+// build_penalty2 through a process-wide cache keyed by (csize, range, wd,
+// wr): the frames of a series share their grid, so each table is built once
+struct Penalty2Table {
+    std::vector<int> rowptr, col;
+    std::vector<float> val;
+};
+std::shared_ptr<const Penalty2Table> penalty2_cached(const int csize[2], const float range[2], double wd, double wr);
 
 }  // namespace mgr
