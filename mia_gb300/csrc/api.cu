@@ -57,6 +57,11 @@ void trace_add(const char *phase, double ms)
     g_trace.push_back({phase, ms, 1});
 }
 
+void trace_count(const char *name, double value)
+{
+    if (trace_enabled()) trace_add(name, value);
+}
+
 void trace_report(const char *title)
 {
     if (!trace_enabled()) return;
@@ -102,6 +107,8 @@ static mgr_status guarded(F f)
         return fail(MGR_ERR_OOM, "device or host allocation failed");
     } catch (const StateError &e) {
         return fail(MGR_ERR_STATE, e.what());
+    } catch (const TimeoutError &e) {
+        return fail(MGR_ERR_TIMEOUT, e.what());
     } catch (const CudaError &e) {
         return fail(MGR_ERR_CUDA, e.what());
     } catch (const std::exception &e) {
@@ -171,6 +178,7 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
             L->own_stream = true;
         }
         L->coef.alloc(L->N, L->stream);
+        L->coef_pad.alloc(pad_floats(d.dim, L->n[0], L->n[1], L->n[2]), L->stream);
         L->ref.alloc(L->N, L->stream);
         L->warped.alloc(L->N, L->stream);
         L->minmax.alloc(2, L->stream);
@@ -266,6 +274,7 @@ void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref
     k_mean_final<<<2, 256, 0, st>>>(L->mpart.p, nb, L->N, L->means.p);
     count_launch(2);
     launch_prefilter(L->coef.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
+    launch_pad_mirror(L->coef.p, L->coef_pad.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
     check_launch("set_images kernels");
     L->images_set = true;
 }
@@ -384,7 +393,10 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
             ck(cudaMemcpyAsync(grad_penalty, lvl->grad_penalty.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
         double c[2];
         ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        unsigned flag = 0;
+        read_status_flag(lvl, &flag);
         ck(cudaStreamSynchronize(st), "evaluate sync");
+        throw_if_flagged(lvl, flag);
         if (cost_image) *cost_image = c[0];
         if (cost_penalty) *cost_penalty = c[1];
     });
@@ -403,7 +415,10 @@ mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_im
         check_launch("value kernels");
         double c[2];
         ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        unsigned flag = 0;
+        read_status_flag(lvl, &flag);
         ck(cudaStreamSynchronize(lvl->stream), "value sync");
+        throw_if_flagged(lvl, flag);
         if (cost_image) *cost_image = c[0];
         if (cost_penalty) *cost_penalty = c[1];
     });
@@ -529,7 +544,10 @@ mgr_status mgr_level_sync(mgr_level *lvl)
     if (!lvl) return fail(MGR_ERR_ARG, "null level");
     return guarded([&] {
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        unsigned flag = 0;
+        read_status_flag(lvl, &flag);
         ck(cudaStreamSynchronize(lvl->stream), "sync");
+        throw_if_flagged(lvl, flag);
     });
 }
 

@@ -287,13 +287,14 @@ struct PairRun {
 void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
+    if (s == MGR_ERR_TIMEOUT) throw TimeoutError(mgr_last_error());
     if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
 }
 
 // Run the minimizer of every pair with in_pass set, in lock step, until all
 // have finished.  Steps are captured into a CUDA graph when use_graphs.
 void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_desc &mz, int dim, int tile[3],
-              bool use_graphs, cudaStream_t st)
+              bool use_graphs, cudaStream_t st, const char *label)
 {
     std::vector<int> members;
     for (size_t i = 0; i < pairs.size(); ++i)
@@ -399,21 +400,36 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         ck(cudaStreamSynchronize(st), "batch sync");
         if (active == 0) break;
     }
+    const auto t_steps0 = tr_steps.t0;
     tr_steps.stop();
+    const double steps_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_steps0).count();
     TraceScope tr_back("batch: readback", st);
     if (exec) cudaGraphExecDestroy(exec);
     ck(cudaMemcpyAsync(states.data(), d_states.p, np * sizeof(MinState), cudaMemcpyDeviceToHost, st), "D2H");
+    std::vector<unsigned> flags(np, 0u);
     for (int k = 0; k < np; ++k) {
         PairRun &r = *pairs[members[k]];
         ck(cudaMemcpyAsync(r.params.data(), r.x.p, r.params.size() * sizeof(double), cudaMemcpyDeviceToHost, st),
            "D2H");
+        read_status_flag(r.lvl, &flags[k]);
     }
     ck(cudaStreamSynchronize(st), "batch sync");
+    for (int k = 0; k < np; ++k) throw_if_flagged(pairs[members[k]]->lvl, flags[k]);
+    double vox_evals = 0.0;
     for (int k = 0; k < np; ++k) {
         PairRun &r = *pairs[members[k]];
         r.cost = states[k].f;
         r.evals += states[k].evals;
+        vox_evals += double(states[k].evals) * double(args[k].n[0]) * args[k].n[1] * args[k].n[2];
         round_params_to_float(r.params);
+    }
+    tr_back.stop();
+    if (trace_enabled()) {
+        const std::string tag = "batch: " + std::string(label) + " ";
+        trace_count((tag + "Mvoxel-evals").c_str(), vox_evals * 1e-6);
+        trace_count((tag + "lock-step steps").c_str(), double(steps));
+        trace_count((tag + "steps ms").c_str(), steps_ms);
     }
 }
 
@@ -540,7 +556,8 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                     level_set_images_async(r.lvl, r.src_l.p, r.ref_l.p);
                 }
                 tr_lvl.stop();
-                run_pass(pairs, *mz, dim, tile, use_graphs != 0, st);
+                const std::string label = "level " + std::to_string(shift) + " pass " + std::to_string(pass);
+                run_pass(pairs, *mz, dim, tile, use_graphs != 0, st, label.c_str());
             }
             for (auto &rp : pairs)
                 for (int k = 0; k < 3; ++k) rp->prev[k] = rp->size[k];
@@ -558,6 +575,9 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
     } catch (const std::invalid_argument &e) {
         set_last_error(e.what());
         return MGR_ERR_ARG;
+    } catch (const TimeoutError &e) {
+        set_last_error(e.what());
+        return MGR_ERR_TIMEOUT;
     } catch (const std::bad_alloc &) {
         set_last_error("allocation failed");
         return MGR_ERR_OOM;

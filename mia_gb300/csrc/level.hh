@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -19,6 +20,10 @@ struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+// a bounded device wait gave up (the kernel raised the level's status flag)
+struct TimeoutError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
@@ -70,32 +75,43 @@ struct DevBuf {
     }
 };
 
+// the per-axis tables of a level, packed with the other tables into one
+// host blob and uploaded with one copy; `off` are byte offsets into it
 struct AxisDev {
     AxisHost h;
-    DevBuf<int> fs, as, rows, ftile0, atile0, gtile;
-    DevBuf<float> fw, aw;
-    void upload(cudaStream_t st)
+    size_t off[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // fs, as, rows, ftile0, atile0, gtile, fw, aw
+    const unsigned char *base = nullptr;
+
+    template <class T>
+    static size_t pack(std::vector<unsigned char> &blob, const std::vector<T> &v)
     {
-        fs.upload(h.fs, st);
-        as.upload(h.as, st);
-        rows.upload(h.rows, st);
-        ftile0.upload(h.ftile0, st);
-        atile0.upload(h.atile0, st);
-        gtile.upload(h.gtile, st);
-        fw.upload(h.fw, st);
-        aw.upload(h.aw, st);
+        const size_t o = (blob.size() + 255) & ~size_t(255);
+        blob.resize(o + v.size() * sizeof(T));
+        if (!v.empty()) std::memcpy(blob.data() + o, v.data(), v.size() * sizeof(T));
+        return o;
+    }
+    void pack_all(std::vector<unsigned char> &blob)
+    {
+        off[0] = pack(blob, h.fs);
+        off[1] = pack(blob, h.as);
+        off[2] = pack(blob, h.rows);
+        off[3] = pack(blob, h.ftile0);
+        off[4] = pack(blob, h.atile0);
+        off[5] = pack(blob, h.gtile);
+        off[6] = pack(blob, h.fw);
+        off[7] = pack(blob, h.aw);
     }
     Axis view() const
     {
         Axis a;
-        a.fs = fs.p;
-        a.fw = reinterpret_cast<const float4 *>(fw.p);
-        a.as = as.p;
-        a.aw = reinterpret_cast<const float4 *>(aw.p);
-        a.rows = reinterpret_cast<const int2 *>(rows.p);
-        a.ftile0 = ftile0.p;
-        a.atile0 = atile0.p;
-        a.gtile = reinterpret_cast<const int2 *>(gtile.p);
+        a.fs = reinterpret_cast<const int *>(base + off[0]);
+        a.as = reinterpret_cast<const int *>(base + off[1]);
+        a.rows = reinterpret_cast<const int2 *>(base + off[2]);
+        a.ftile0 = reinterpret_cast<const int *>(base + off[3]);
+        a.atile0 = reinterpret_cast<const int *>(base + off[4]);
+        a.gtile = reinterpret_cast<const int2 *>(base + off[5]);
+        a.fw = reinterpret_cast<const float4 *>(base + off[6]);
+        a.aw = reinterpret_cast<const float4 *>(base + off[7]);
         a.n = h.n;
         a.nc = h.nc;
         a.t = h.t;
@@ -120,7 +136,8 @@ struct mgr_level {
     int path = MGR_PATH_SPLIT;
     int tile[3] = {32, 8, 8};
     AxisDev ax[3];
-    DevBuf<float> coef, ref, warped, minmax, partial, ptable, pen_val;
+    DevBuf<unsigned char> axis_tables;   // the packed AxisDev tables
+    DevBuf<float> coef, coef_pad, ref, warped, minmax, partial, ptable, pen_val;
     DevBuf<float2> mmpart;
     DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means, mpart;
     DevBuf<unsigned int> counters;
@@ -152,6 +169,8 @@ struct mgr_level {
             a.ax[k] = ax[k].view();
         }
         a.coef_img = coef.p;
+        a.coef_pad = coef_pad.p;
+        a.pad_rows = n[1] + 2 * PAD_H;
         a.ref = ref.p;
         a.warped = warped.p;
         a.minmax = minmax.p;
@@ -184,10 +203,15 @@ struct mgr_level {
     void build_tables()
     {
         const int D = d.dim;
+        std::vector<unsigned char> blob;
         for (int k = 0; k < D; ++k) {
             build_axis(ax[k].h, n[k], nc[k], tile[k]);
-            ax[k].upload(stream);
+            ax[k].pack_all(blob);
         }
+        // a fresh buffer: kernels queued earlier may still read the old one
+        axis_tables.release();
+        axis_tables.upload(blob, stream);
+        for (int k = 0; k < D; ++k) ax[k].base = axis_tables.p;
         const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
         slot = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
         partial.alloc(size_t(ntiles) * slot, stream);
@@ -201,4 +225,21 @@ struct mgr_level {
 namespace mgr {
 // mgr_level_set_images_device without the final stream synchronisation
 void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref);
+}  // namespace mgr
+
+namespace mgr {
+// Queue a read of the level's device status flag (counters[6], raised by a
+// kernel whose bounded wait gave up) into *flag; after the stream has been
+// synchronised, throw_if_flagged clears it and throws TimeoutError.
+inline void read_status_flag(mgr_level *L, unsigned *flag)
+{
+    ck(cudaMemcpyAsync(flag, L->counters.p + 6, sizeof(unsigned), cudaMemcpyDeviceToHost, L->stream), "status D2H");
+}
+inline void throw_if_flagged(mgr_level *L, unsigned flag)
+{
+    if (flag) {
+        ck(cudaMemsetAsync(L->counters.p + 6, 0, sizeof(unsigned), L->stream), "status reset");
+        throw TimeoutError("a bounded device wait gave up (bulk copy did not complete)");
+    }
+}
 }  // namespace mgr

@@ -35,6 +35,39 @@ __device__ __forceinline__ void bspline3_weights(float f, float w[4])
     w[2] = ((f - w3) - w3) + w0;
 }
 
+// Mirror halo of the padded copy of the prefiltered moving image that the
+// split path's warp kernel stages from (voxels per side; the padded rows are
+// 128-byte aligned so that any 16-byte aligned row segment can be copied
+// with one bulk copy).
+constexpr int PAD_H = 16;
+
+__host__ __device__ inline int pad_pitch(int nx)
+{
+    return ((nx + 2 * PAD_H + 31) / 32) * 32;
+}
+
+// Shared-memory box in which the warp kernel stages the moving image's tap
+// footprint of one tile: rows of stage_bx floats (a multiple of 32, so that
+// the bank of a tap depends only on its x position and lanes on different
+// rows do not conflict), stage_by rows per plane, stage_bz planes.  A tile
+// whose footprint does not fit reads its taps from global memory.
+__host__ __device__ constexpr int stage_bx(int tx)
+{
+    return ((tx + 24 + 31) / 32) * 32;
+}
+__host__ __device__ constexpr int stage_by(int ty)
+{
+    return ty + 10;
+}
+__host__ __device__ constexpr int stage_bz(int dim, int tz)
+{
+    return dim == 3 ? tz + 10 : 1;
+}
+__host__ __device__ constexpr int stage_floats(int dim, int tx, int ty, int tz)
+{
+    return stage_bx(tx) * stage_by(ty) * stage_bz(dim, tz);
+}
+
 // Mirror boundary index folding with period 2w-2
 // (mia/core/splinebc/bc.cc:52-64).
 __device__ __forceinline__ int mirror_fold(int i, int w)
@@ -135,6 +168,50 @@ __device__ __forceinline__ float sample2(const float *__restrict__ c, int nx, in
         const float *__restrict__ row = c + iy[ky];
         const float r = wx[0] * __ldg(row + ix[0]) + wx[1] * __ldg(row + ix[1]) +
                         wx[2] * __ldg(row + ix[2]) + wx[3] * __ldg(row + ix[3]);
+        acc += wy[ky] * r;
+    }
+    return clamp_ref(acc, mn, mx);
+}
+
+// Tricubic / bicubic sample from a shared-memory footprint of the
+// prefiltered image whose elements already hold the mirror-folded values:
+// `base` points at the first tap (fx-1, fy-1, fz-1) and rows / planes are
+// `sy` / `sz` floats apart.  Same weights and summation order as sample3 /
+// sample2.
+__device__ __forceinline__ float staged_sample3(const float *base, int sy, int sz, float px, float py, float pz,
+                                                int fx, int fy, int fz, float mn, float mx)
+{
+    float wx[4], wy[4], wz[4];
+    bspline3_weights(px - float(fx), wx);
+    bspline3_weights(py - float(fy), wy);
+    bspline3_weights(pz - float(fz), wz);
+    float acc = 0.0f;
+#pragma unroll
+    for (int kz = 0; kz < 4; ++kz) {
+        const float *pl = base + kz * sz;
+        float ay = 0.0f;
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky) {
+            const float *row = pl + ky * sy;
+            const float r = wx[0] * row[0] + wx[1] * row[1] + wx[2] * row[2] + wx[3] * row[3];
+            ay += wy[ky] * r;
+        }
+        acc += wz[kz] * ay;
+    }
+    return clamp_ref(acc, mn, mx);
+}
+
+__device__ __forceinline__ float staged_sample2(const float *base, int sy, float px, float py, int fx, int fy,
+                                                float mn, float mx)
+{
+    float wx[4], wy[4];
+    bspline3_weights(px - float(fx), wx);
+    bspline3_weights(py - float(fy), wy);
+    float acc = 0.0f;
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+        const float *row = base + ky * sy;
+        const float r = wx[0] * row[0] + wx[1] * row[1] + wx[2] * row[2] + wx[3] * row[3];
         acc += wy[ky] * r;
     }
     return clamp_ref(acc, mn, mx);

@@ -15,6 +15,10 @@ void count_launch(unsigned n = 1);
 void count_launch_adjust(unsigned long long value);
 
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
+// padded copy with the mirror fold applied in the halo (layout of coef_pad)
+void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st);
+// the padded image's size in floats
+size_t pad_floats(int dim, int nx, int ny, int nz);
 void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
                    float *out, cudaStream_t st);
 
@@ -25,6 +29,8 @@ struct EvalArgs {
     int nc[3];             // coefficient grid
     Axis ax[3];            // per-axis tables (ax[2] unused in 2D)
     const float *coef_img; // prefiltered moving image
+    const float *coef_pad; // the same with a mirror halo of PAD_H voxels (3D: all axes, 2D: x and y)
+    int pad_rows;          // rows per plane of coef_pad (ny + 2 PAD_H); the row pitch is pad_pitch(nx)
     const float *ref;      // reference image
     float *warped;         // warped moving image (N)
     const float *minmax;   // device {min, max} clamp bounds

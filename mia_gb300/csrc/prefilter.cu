@@ -5,6 +5,7 @@
 // (mia/core/boundary_conditions.cc:62-103) and CMirrorOnBoundary
 // (mia/core/splinebc/bc.cc:67-88): x lines, then y lines, then z lines, each
 // line filtered in double and stored back as float.
+#include <algorithm>
 #include "mgr_common.cuh"
 #include "mgr_kernels.hh"
 
@@ -151,6 +152,39 @@ void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t 
         k_prefilter_lines<<<dim3((nx + lb - 1) / lb, ny), 32, sm, st>>>(img, nx, ny, nz, 2, lb);
         count_launch();
     }
+}
+
+__global__ void k_pad_mirror(const float *__restrict__ img, float *__restrict__ pad, int nx, int ny, int nz,
+                             int pitch, int rows, int hz, size_t total)
+{
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int px = int(i % pitch);
+        const size_t r = i / pitch;
+        const int py = int(r % rows), pz = int(r / rows);
+        const int x = px - PAD_H, y = py - PAD_H, z = pz - hz;
+        float v = 0.0f;
+        if (x < nx + PAD_H) {
+            const int gx = mirror_fold(x, nx), gy = mirror_fold(y, ny), gz = mirror_fold(z, nz);
+            v = img[(size_t(gz) * ny + gy) * nx + gx];
+        }
+        pad[i] = v;
+    }
+}
+
+size_t pad_floats(int dim, int nx, int ny, int nz)
+{
+    const int planes = dim == 3 ? nz + 2 * PAD_H : 1;
+    return size_t(pad_pitch(nx)) * (ny + 2 * PAD_H) * planes;
+}
+
+void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st)
+{
+    if (dim == 2) nz = 1;
+    const size_t total = pad_floats(dim, nx, ny, nz);
+    const int nb = int(std::min<size_t>(4096, (total + 255) / 256));
+    k_pad_mirror<<<nb, 256, 0, st>>>(img, pad, nx, ny, nz, pad_pitch(nx), ny + 2 * PAD_H, dim == 3 ? PAD_H : 0,
+                                     total);
+    count_launch();
 }
 
 void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,

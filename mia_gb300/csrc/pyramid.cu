@@ -7,10 +7,13 @@
 // * the `scale` filter that builds each multiresolution level
 //   (C3DScale / C2DScale, mia/3d/filter/scale.cc:95-155,
 //   mia/2d/filter/scale.cc:50-90; C1DScalar::downscale,
-//   mia/core/scaler1d.cc): per axis and per line, in double, a binomial
+//   mia/core/scaler1d.cc): per axis and per line a binomial
 //   "gauss:w=round(1/scale)" smoothing with half-sample symmetric borders
 //   (mia/core/spacialkernel/gauss.cc), the mirror-boundary cubic prefilter,
-//   and cubic B-spline resampling at i*(n_in-1)/(n_out-1).
+//   and cubic B-spline resampling at i*(n_in-1)/(n_out-1).  The reference
+//   filters in double; here the lines are filtered in float (FP64 runs at a
+//   small fraction of the FP32 rate on this GPU), which moves the result by
+//   a few float ulp: the parity tests bound it at 1e-5 of the image maximum.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -50,67 +53,94 @@ __global__ void k_apply_linear(const float *__restrict__ in, float *__restrict__
         out[i] = float(fma(a, double(in[i]), b));
 }
 
-// one thread per line; the line and its smoothed copy are staged in shared
-// memory as double (lb lines per block, pitch n_in)
-template <class TI, class TO>
-__global__ void __launch_bounds__(32) k_scale_lines(const TI *__restrict__ in, TO *__restrict__ out, int lb,
+// One warp per block, one line per thread (lb <= 32 lines per block), in
+// float.  The lines are staged in shared memory with an odd pitch; loads and
+// stores are coalesced along x for the x pass (element stride 1) and across
+// the lines otherwise.  Per line: binomial smoothing with half-sample
+// symmetric borders into s, the mirror-boundary cubic prefilter on s in
+// place, then the 4-tap resampling into c (n_out <= n_in).
+__global__ void __launch_bounds__(32) k_scale_lines(const float *__restrict__ in, float *__restrict__ out, int lb,
                                                     int n_in, int n_out, int nlines, size_t in_line_stride,
                                                     size_t in_elem_stride, size_t out_line_stride,
                                                     size_t out_elem_stride, int lines_per_plane,
                                                     size_t in_plane_stride, size_t out_plane_stride, int gw,
-                                                    const double *gmask, const int4 *idx, const Wt4 *wts)
+                                                    const float *gmask, const int4 *idx, const float4 *wts)
 {
-    extern __shared__ double sl[];
+    extern __shared__ float sl[];
+    const int pitch = n_in | 1;
     const int t = threadIdx.x;
-    const int l = blockIdx.x * lb + t;
-    if (t >= lb || l >= nlines) return;
-    double *c = sl + size_t(t) * 2 * n_in;
-    double *s = c + n_in;
-    const int pl = l / lines_per_plane, lp = l % lines_per_plane;
-    const TI *src = in + size_t(pl) * in_plane_stride + size_t(lp) * in_line_stride;
-    TO *dst = out + size_t(pl) * out_plane_stride + size_t(lp) * out_line_stride;
-    for (int k = 0; k < n_in; ++k) c[k] = double(src[k * in_elem_stride]);
-    // binomial smoothing, half-sample symmetric borders
-    if (gw < 0) {  // C1DScalar copies when the size does not change
-        for (int i = 0; i < n_out; ++i) dst[i * out_elem_stride] = TO(c[i]);
-        return;
-    }
-    const int m = 2 * gw + 1;
-    for (int i = 0; i < n_in; ++i) {
-        double h = 0.0;
-        for (int j = 0; j < m; ++j) {
-            int k = i - gw + j;
-            if (k < 0) k = -k - 1;
-            if (k >= n_in) k = 2 * n_in - 1 - k;
-            h += gmask[j] * c[k];
+    const int l0 = blockIdx.x * lb;
+    const int nl = min(lb, nlines - l0);
+    auto line_in = [&](int l) {
+        const int g = l0 + l, pl = g / lines_per_plane, lp = g % lines_per_plane;
+        return in + size_t(pl) * in_plane_stride + size_t(lp) * in_line_stride;
+    };
+    auto line_out = [&](int l) {
+        const int g = l0 + l, pl = g / lines_per_plane, lp = g % lines_per_plane;
+        return out + size_t(pl) * out_plane_stride + size_t(lp) * out_line_stride;
+    };
+    float *c_all = sl;
+    float *s_all = sl + size_t(lb) * pitch;
+    if (in_elem_stride == 1) {
+        for (int l = 0; l < nl; ++l) {
+            const float *src = line_in(l);
+            for (int k = t; k < n_in; k += 32) c_all[l * pitch + k] = src[k];
         }
-        s[i] = h;
+    } else if (t < nl) {
+        const float *src = line_in(t);
+        for (int k = 0; k < n_in; ++k) c_all[t * pitch + k] = src[k * in_elem_stride];
     }
-    // mirror-boundary prefilter (filter_line), in double
-    if (n_in >= 2) {
-        const double p = 1.7320508075688772 - 2.0;
-        const double lambda = 2.0 - p - 1.0 / p;
-        for (int k = 0; k < n_in; ++k) s[k] *= lambda;
-        double zn = p;
-        const double iz = 1.0 / p;
-        double z2n = pow(p, double(n_in - 1));
-        double sum = s[0] + z2n * s[n_in - 1];
-        z2n *= z2n * iz;
-        for (int k = 1; k < n_in - 1; ++k) {
-            sum += (zn + z2n) * s[k];
-            zn *= p;
-            z2n *= iz;
+    __syncwarp();
+    if (t < nl) {
+        float *c = c_all + t * pitch;
+        float *s = s_all + t * pitch;
+        if (gw >= 0) {  // (C1DScalar copies when the size does not change: c is the output)
+            const int m = 2 * gw + 1;
+            for (int i = 0; i < n_in; ++i) {
+                float h = 0.0f;
+                for (int j = 0; j < m; ++j) {
+                    int k = i - gw + j;
+                    if (k < 0) k = -k - 1;
+                    if (k >= n_in) k = 2 * n_in - 1 - k;
+                    h = fmaf(gmask[j], c[k], h);
+                }
+                s[i] = h;
+            }
+            if (n_in >= 2) {
+                const float p = -0.2679491924311227f;            // sqrt(3) - 2
+                const float lambda = 6.0f;                       // 2 - p - 1/p
+                for (int k = 0; k < n_in; ++k) s[k] *= lambda;
+                float zn = p;
+                const float iz = 1.0f / p;
+                float z2n = powf(p, float(n_in - 1));
+                float sum = fmaf(z2n, s[n_in - 1], s[0]);
+                z2n *= z2n * iz;
+                for (int k = 1; k < n_in - 1; ++k) {
+                    sum = fmaf(zn + z2n, s[k], sum);
+                    zn *= p;
+                    z2n *= iz;
+                }
+                s[0] = sum / (1.0f - zn * zn);
+                for (int k = 1; k < n_in; ++k) s[k] = fmaf(p, s[k - 1], s[k]);
+                s[n_in - 1] = (p / (p * p - 1.0f)) * fmaf(p, s[n_in - 2], s[n_in - 1]);
+                for (int k = n_in - 2; k >= 0; --k) s[k] = p * (s[k + 1] - s[k]);
+            }
+            for (int i = 0; i < n_out; ++i) {
+                const int4 ix = idx[i];
+                const float4 w = wts[i];
+                c[i] = fmaf(w.x, s[ix.x], fmaf(w.y, s[ix.y], fmaf(w.z, s[ix.z], w.w * s[ix.w])));
+            }
         }
-        s[0] = sum / (1.0 - zn * zn);
-        for (int k = 1; k < n_in; ++k) s[k] += p * s[k - 1];
-        s[n_in - 1] = (p / (p * p - 1.0)) * (p * s[n_in - 2] + s[n_in - 1]);
-        for (int k = n_in - 2; k >= 0; --k) s[k] = p * (s[k + 1] - s[k]);
     }
-    for (int i = 0; i < n_out; ++i) {
-        const int4 ix = idx[i];
-        const Wt4 w = wts[i];
-        const double v = w.x * s[ix.x] + w.y * s[ix.y] + w.z * s[ix.z] + w.w * s[ix.w];
-        dst[i * out_elem_stride] = TO(v);
+    __syncwarp();
+    if (out_elem_stride == 1) {
+        for (int l = 0; l < nl; ++l) {
+            float *dst = line_out(l);
+            for (int k = t; k < n_out; k += 32) dst[k] = c_all[l * pitch + k];
+        }
+    } else if (t < nl) {
+        float *dst = line_out(t);
+        for (int k = 0; k < n_out; ++k) dst[k * out_elem_stride] = c_all[t * pitch + k];
     }
 }
 
@@ -191,32 +221,37 @@ AxisPlan plan_axis(int n_in, int n_out)
     return p;
 }
 
-template <class TI, class TO>
-void scale_axis(const TI *in, TO *out, const AxisPlan &p, int n_in, int n_out, int nlines, size_t ils, size_t ies,
-                size_t ols, size_t oes, int lpp, size_t ips, size_t ops, cudaStream_t st)
+void scale_axis(const float *in, float *out, const AxisPlan &p, int n_in, int n_out, int nlines, size_t ils,
+                size_t ies, size_t ols, size_t oes, int lpp, size_t ips, size_t ops, cudaStream_t st)
 {
-    // stream-ordered temporaries; the plan's host vectors may go away once
-    // the (pageable) copies have been issued
-    double *d_mask = nullptr;
-    int4 *d_idx = nullptr;
-    Wt4 *d_wts = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_mask), p.mask.size() * sizeof(double), st), "cudaMallocAsync");
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_idx), p.idx.size() * sizeof(int4), st), "cudaMallocAsync");
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_wts), p.wts.size() * sizeof(Wt4), st), "cudaMallocAsync");
-    ck(cudaMemcpyAsync(d_mask, p.mask.data(), p.mask.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
-    ck(cudaMemcpyAsync(d_idx, p.idx.data(), p.idx.size() * sizeof(int4), cudaMemcpyHostToDevice, st), "H2D");
-    ck(cudaMemcpyAsync(d_wts, p.wts.data(), p.wts.size() * sizeof(Wt4), cudaMemcpyHostToDevice, st), "H2D");
+    // the plan (mask, taps, weights) as float in one stream-ordered upload;
+    // the host blob may go away once the pageable copy has been issued
+    std::vector<float> mask(p.mask.begin(), p.mask.end());
+    std::vector<float4> wts;
+    for (const Wt4 &w : p.wts) wts.push_back(make_float4(float(w.x), float(w.y), float(w.z), float(w.w)));
+    const size_t o_idx = ((mask.size() * sizeof(float) + 15) / 16) * 16;
+    const size_t o_wts = o_idx + p.idx.size() * sizeof(int4);
+    const size_t bytes = o_wts + wts.size() * sizeof(float4);
+    std::vector<unsigned char> blob(bytes, 0);
+    std::memcpy(blob.data(), mask.data(), mask.size() * sizeof(float));
+    std::memcpy(blob.data() + o_idx, p.idx.data(), p.idx.size() * sizeof(int4));
+    std::memcpy(blob.data() + o_wts, wts.data(), wts.size() * sizeof(float4));
+    unsigned char *d = nullptr;
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
+    ck(cudaMemcpyAsync(d, blob.data(), bytes, cudaMemcpyHostToDevice, st), "H2D");
+    const int pitch = n_in | 1;
     int lb = 32;
-    while (lb > 1 && size_t(lb) * 2 * n_in * sizeof(double) > 160 * 1024) lb >>= 1;
-    const size_t sm = size_t(lb) * 2 * n_in * sizeof(double);
-    cudaFuncSetAttribute(k_scale_lines<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    k_scale_lines<TI, TO><<<(nlines + lb - 1) / lb, 32, sm, st>>>(in, out, lb, n_in, n_out, nlines, ils, ies, ols, oes,
-                                                                  lpp, ips, ops, p.gw, d_mask, d_idx, d_wts);
+    while (lb > 1 && size_t(lb) * 2 * pitch * sizeof(float) > 200 * 1024) lb >>= 1;
+    const size_t sm = size_t(lb) * 2 * pitch * sizeof(float);
+    if (sm > 200 * 1024) throw std::invalid_argument("scale: image line too long");
+    cudaFuncSetAttribute(k_scale_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_scale_lines<<<(nlines + lb - 1) / lb, 32, sm, st>>>(in, out, lb, n_in, n_out, nlines, ils, ies, ols, oes, lpp,
+                                                         ips, ops, p.gw, reinterpret_cast<const float *>(d),
+                                                         reinterpret_cast<const int4 *>(d + o_idx),
+                                                         reinterpret_cast<const float4 *>(d + o_wts));
     count_launch();
     ck(cudaGetLastError(), "scale kernel");
-    cudaFreeAsync(d_mask, st);
-    cudaFreeAsync(d_idx, st);
-    cudaFreeAsync(d_wts, st);
+    cudaFreeAsync(d, st);
 }
 
 }  // namespace
@@ -275,23 +310,20 @@ void scale_image(const float *d_in, const int in_size[3], float *d_out, const in
     for (int k = 0; k < dim; ++k)
         if (out_size[k] > in_size[k] || out_size[k] < 2)
             throw std::invalid_argument("scale: only downscaling to sizes >= 2 is supported");
-    // x: float -> double, lines = rows (y, z)
-    double *t1 = nullptr, *t2 = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&t1), size_t(mx) * ny * nz * sizeof(double), st), "cudaMallocAsync");
+    // x: lines = rows (y, z)
+    float *t1 = nullptr, *t2 = nullptr;
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&t1), size_t(mx) * ny * nz * sizeof(float), st), "cudaMallocAsync");
     const AxisPlan px = plan_axis(nx, mx);
     const AxisPlan py = plan_axis(ny, my);
-    // C1DScalar copies when the size does not change on an axis
-    auto run_x = [&](auto *out) {
-        scale_axis(d_in, out, px, nx, mx, ny * nz, size_t(nx), 1, size_t(mx), 1, ny * nz, 0, 0, st);
-    };
-    run_x(t1);
+    // (C1DScalar copies when the size does not change on an axis)
+    scale_axis(d_in, t1, px, nx, mx, ny * nz, size_t(nx), 1, size_t(mx), 1, ny * nz, 0, 0, st);
     if (dim == 2) {
-        // y: double -> float, lines = columns x, stride mx
+        // y: lines = columns x, stride mx
         scale_axis(t1, d_out, py, ny, my, mx, 1, size_t(mx), 1, size_t(mx), mx, 0, 0, st);
         cudaFreeAsync(t1, st);
         return;
     }
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&t2), size_t(mx) * my * nz * sizeof(double), st), "cudaMallocAsync");
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&t2), size_t(mx) * my * nz * sizeof(float), st), "cudaMallocAsync");
     // y: lines = (x, z): per plane z, mx lines of stride 1, element stride mx
     scale_axis(t1, t2, py, ny, my, mx * nz, 1, size_t(mx), 1, size_t(mx), mx, size_t(mx) * ny, size_t(mx) * my, st);
     // z: lines = (x, y): mx*my lines, element stride mx*my

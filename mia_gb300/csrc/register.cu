@@ -24,6 +24,7 @@ namespace {
 void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
+    if (s == MGR_ERR_TIMEOUT) throw TimeoutError(mgr_last_error());
     if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
 }
 
@@ -173,6 +174,9 @@ extern "C" mgr_status mgr_register(const mgr_level_desc *desc, int levels, const
     } catch (const std::invalid_argument &e) {
         set_last_error(e.what());
         return MGR_ERR_ARG;
+    } catch (const TimeoutError &e) {
+        set_last_error(e.what());
+        return MGR_ERR_TIMEOUT;
     } catch (const std::bad_alloc &) {
         set_last_error("allocation failed");
         return MGR_ERR_OOM;

@@ -85,9 +85,12 @@ __device__ __forceinline__ void window_contract(int len, const int *start, const
 template <int D, int TX, int TY, int TZ>
 __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int bz, int ntiles, int tile)
 {
-    extern __shared__ float sm[];
+    static_assert(NT % TX == 0, "a thread keeps its x column");
+    extern __shared__ __align__(128) float sm[];
     __shared__ double red[5 * (NT / 32)];
+    __shared__ float cred[NT / 32][6];
     __shared__ bool is_last;
+    __shared__ __align__(8) unsigned long long mbar;
     __shared__ int fsx[TX], fsy[TY], fsz[TZ];
     __shared__ float4 fwx[TX], fwy[TY], fwz[TZ];
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
@@ -97,12 +100,19 @@ __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int
     const int FX = X.fc, FY = Y.fc, FZ = (D == 3) ? Z.fc : 1;
     const int cx0 = X.ftile0[bx], cy0 = Y.ftile0[by], cz0 = (D == 3) ? Z.ftile0[bz] : 0;
     const int ncx = a.nc[0], ncy = a.nc[1], ncz = (D == 3) ? a.nc[2] : 1;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
     float *C = sm;                                       // [D][FZ][FY][FX]
     float *T1 = C + D * FZ * FY * FX;                    // [D][TZ][FY][FX]   (3D)
     float *T2 = T1 + ((D == 3) ? D * TZ * FY * FX : 0);  // [D][TZ][TY][FX]
+    // after C, T1, T2, rounded up to 32 floats (the host sizes it the same way)
+    float *Fp = sm + ((D * FZ * FY * FX + ((D == 3) ? D * TZ * FY * FX : 0) + D * TZ * TY * FX + 31) & ~31);
 
+    if (tid == 0) {
+        const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(&mbar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
     // per-tile forward tables (voxels past the image edge repeat the last one)
     if (tid < TX) {
         const int x = min(x0 + tid, nx - 1);
@@ -149,7 +159,11 @@ __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int
         }
         __syncthreads();
     }
+    // y stage.  The displacement of every voxel of the tile is a convex
+    // combination (partition-of-unity weights) of the T2 entries of its
+    // component, so their per-component range bounds the sample points.
     {
+        float cmin[3] = {3.4e38f, 3.4e38f, 3.4e38f}, cmax[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
         const float *Src = (D == 3) ? T1 : C;  // [D][TZ][FY][FX] (2D: TZ = FZ = 1)
         if (m.act) {
             for (int r = m.r0; r < D * TZ * TY; r += m.rstep) {
@@ -158,34 +172,146 @@ __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int
                 const int s = fsy[yy];
                 const float4 w = fwy[yy];
                 const float *c = Src + ((comp * TZ + zz) * FY + s) * FX + m.ix;
-                T2[r * FX + m.ix] = w.x * c[0] + w.y * c[FX] + w.z * c[2 * FX] + w.w * c[3 * FX];
+                const float v = w.x * c[0] + w.y * c[FX] + w.z * c[2 * FX] + w.w * c[3 * FX];
+                T2[r * FX + m.ix] = v;
+#pragma unroll
+                for (int k = 0; k < D; ++k)
+                    if (comp == k) {
+                        cmin[k] = fminf(cmin[k], v);
+                        cmax[k] = fmaxf(cmax[k], v);
+                    }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                cmin[k] = fminf(cmin[k], __shfl_xor_sync(0xffffffffu, cmin[k], o));
+                cmax[k] = fmaxf(cmax[k], __shfl_xor_sync(0xffffffffu, cmax[k], o));
+            }
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                cred[wid][k] = cmin[k];
+                cred[wid][3 + k] = cmax[k];
             }
         }
     }
     __syncthreads();
 
-    // x stage, tricubic sample, warped image, sums
+    // footprint of the interpolation taps.  A sample point x - u(x) lies in
+    // [x_lo - max T2, x_hi - min T2] per axis (plus a rounding margin); its taps
+    // span [floor - 1, floor + 3].  The box is staged from the padded image
+    // when it lies within the halo and fits the shared-memory budget.
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    bool staged = true;
+    {
+        const int v0[3] = {x0, y0, z0}, v1[3] = {x0 + ex - 1, y0 + ey - 1, z0 + ez - 1};
+        const int nn[3] = {nx, ny, nz};
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            float c0 = cred[0][k], c1 = cred[0][3 + k];
+            for (int w = 1; w < NT / 32; ++w) {
+                c0 = fminf(c0, cred[w][k]);
+                c1 = fmaxf(c1, cred[w][3 + k]);
+            }
+            const float mg = 0.01f + 1e-5f * (fabsf(c0) + fabsf(c1) + float(v1[k]));
+            const float pmin = float(v0[k]) - c1 - mg, pmax = float(v1[k]) - c0 + mg;
+            if (!(pmin > -1e6f && pmax < 1e6f)) {
+                staged = false;
+                continue;
+            }
+            lo[k] = int(floorf(pmin)) - 1;
+            hi[k] = int(floorf(pmax)) + 3;
+            if (lo[k] < -PAD_H || hi[k] > nn[k] - 1 + PAD_H) staged = false;
+        }
+        if (D == 2) lo[2] = hi[2] = 0;
+    }
+    // x origin aligned to 16 bytes in the padded rows; row length in floats
+    constexpr int SBX = stage_bx(TX), SBY = stage_by(TY), SBZ = stage_bz(D, TZ);
+    const int sx0 = ((lo[0] + PAD_H) & ~3) - PAD_H;
+    const int SP = ((hi[0] - sx0 + 1) + 3) & ~3;
+    const int FPY = hi[1] - lo[1] + 1, FPZ = hi[2] - lo[2] + 1;
+    if (staged && (SP > SBX || FPY > SBY || FPZ > SBZ)) staged = false;
+    const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(&mbar));
+    if (staged && wid == 0) {
+        // one bulk copy per footprint row (16-byte aligned, multiple of 16
+        // bytes), completion counted on the mbarrier
+        const int rows = FPY * FPZ;
+        if (lane == 0) {
+            const unsigned bytes = unsigned(rows) * unsigned(SP) * 4u;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
+        }
+        __syncwarp();
+        const int P = pad_pitch(nx), PY = a.pad_rows;
+        const int hz = (D == 3) ? PAD_H : 0;
+        for (int r = lane; r < rows; r += 32) {
+            const int j = r % FPY, k = r / FPY;
+            const float *src = a.coef_pad + (size_t(lo[2] + k + hz) * PY + (lo[1] + j + PAD_H)) * P + (sx0 + PAD_H);
+            const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(Fp + (k * SBY + j) * SBX));
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                         "l"(src), "r"(unsigned(SP) * 4u), "r"(mb)
+                         : "memory");
+        }
+    }
+    __syncthreads();
+    if (staged) {
+        // bounded wait for the copies (phase 0); on time-out the status flag
+        // is raised and the copies are waited for once more before the block
+        // may leave
+        unsigned done = 0;
+        for (int it = 0; it < (1 << 22) && !done; ++it)
+            asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done)
+                         : "r"(mb)
+                         : "memory");
+        if (!done) {
+            atomicOr(&a.counters[6], 1u);
+            for (int it = 0; it < (1 << 22) && !done; ++it)
+                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                             : "=r"(done)
+                             : "r"(mb)
+                             : "memory");
+        }
+    }
+
+    // x stage, tricubic sample, warped image, sums: a thread keeps its x
+    // column and walks the rows (y, z) of the tile
     float acc[5] = {0, 0, 0, 0, 0};
     const float mn = a.minmax[0], mxv = a.minmax[1];
     const float ca = float(a.centers[0]), cb = float(a.centers[1]);
-    constexpr int NV = TX * TY * TZ;
-    for (int v = tid; v < NV; v += NT) {
-        const int xx = v % TX, yy = (v / TX) % TY, zz = v / (TX * TY);
+    const int xx = tid % TX;
+    const int x = x0 + xx;
+    const int s = fsx[xx];
+    const float4 w = fwx[xx];
+    for (int r = tid / TX; r < TY * TZ; r += NT / TX) {
+        const int yy = r % TY, zz = r / TY;
         if (xx >= ex || yy >= ey || zz >= ez) continue;
-        const int x = x0 + xx, y = y0 + yy, z = z0 + zz;
-        const int s = fsx[xx];
-        const float4 w = fwx[xx];
-        float u[3];
+        const int y = y0 + yy, z = z0 + zz;
+        float p[3];
 #pragma unroll
         for (int comp = 0; comp < D; ++comp) {
             const float *c = T2 + ((comp * TZ + zz) * TY + yy) * FX + s;
-            u[comp] = w.x * c[0] + w.y * c[1] + w.z * c[2] + w.w * c[3];
+            const float u = w.x * c[0] + w.y * c[1] + w.z * c[2] + w.w * c[3];
+            p[comp] = float(comp == 0 ? x : (comp == 1 ? y : z)) - u;
         }
+        const int fx = ffloor16(p[0]), fy = ffloor16(p[1]), fz = (D == 3) ? ffloor16(p[2]) : 0;
         float wv;
-        if (D == 3)
-            wv = sample3(a.coef_img, nx, ny, nz, float(x) - u[0], float(y) - u[1], float(z) - u[2], mn, mxv);
-        else
-            wv = sample2(a.coef_img, nx, ny, float(x) - u[0], float(y) - u[1], mn, mxv);
+        const bool in_box = staged && fx - 1 >= lo[0] && fx + 2 <= hi[0] && fy - 1 >= lo[1] && fy + 2 <= hi[1] &&
+                            (D == 2 || (fz - 1 >= lo[2] && fz + 2 <= hi[2]));
+        if (in_box) {
+            const int pz = (D == 3) ? fz - 1 - lo[2] : 0;
+            const float *base = Fp + (pz * SBY + (fy - 1 - lo[1])) * SBX + (fx - 1 - sx0);
+            if (D == 3)
+                wv = staged_sample3(base, SBX, SBX * SBY, p[0], p[1], p[2], fx, fy, fz, mn, mxv);
+            else
+                wv = staged_sample2(base, SBX, p[0], p[1], fx, fy, mn, mxv);
+        } else if (D == 3) {
+            wv = sample3(a.coef_img, nx, ny, nz, p[0], p[1], p[2], mn, mxv);
+        } else {
+            wv = sample2(a.coef_img, nx, ny, p[0], p[1], mn, mxv);
+        }
         const size_t idx = (size_t(z) * ny + y) * nx + x;
         a.warped[idx] = wv;
         const float b = a.ref[idx];
@@ -225,7 +351,7 @@ __device__ __forceinline__ void warp_body(const EvalArgs &a, int bx, int by, int
 template <int D, int TX, int TY, int TZ>
 __device__ __forceinline__ void adjoint_body(const EvalArgs &a, int bx, int by, int bz, int tile_index)
 {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(128) float sm[];
     constexpr int HX = TX + 2, HY = TY + 2, HZ = (D == 3) ? TZ + 2 : 1;
     constexpr int TXP = TX + 1;
     __shared__ int asx[TX], asy[TY], asz[TZ];
@@ -396,6 +522,8 @@ static size_t warp_smem(const EvalArgs &a)
     size_t f = size_t(D) * FZ * Y.fc * X.fc;
     if (D == 3) f += size_t(D) * TZ * Y.fc * X.fc;
     f += size_t(D) * TZ * Y.t * X.fc;
+    f = (f + 31) & ~size_t(31);
+    f += stage_floats(D, X.t, Y.t, D == 3 ? Z.t : 1);
     return f * sizeof(float);
 }
 

@@ -12,6 +12,8 @@ namespace mgr {
 
 bool trace_enabled();
 void trace_add(const char *phase, double ms);
+// a counted quantity (reported like a phase, in its own unit)
+void trace_count(const char *name, double value);
 void trace_report(const char *title);
 
 struct TraceScope {
