@@ -167,6 +167,8 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
             L->tile[0] = 32;
             L->tile[1] = 16;
             L->tile[2] = 1;
+        } else {
+            L->choose_tile3();
         }
         L->device = device;
         ck(cudaSetDevice(device), "cudaSetDevice");
@@ -178,7 +180,10 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
             L->own_stream = true;
         }
         L->coef.alloc(L->N, L->stream);
-        L->coef_pad.alloc(pad_floats(d.dim, L->n[0], L->n[1], L->n[2]), L->stream);
+        if (d.dim == 2)
+            L->coef_pad.alloc(pad_floats(d.dim, L->n[0], L->n[1], L->n[2]), L->stream);
+        else
+            L->brick.alloc(brick_pairs(L->n[0], L->n[1], L->n[2]), L->stream);
         L->ref.alloc(L->N, L->stream);
         L->warped.alloc(L->N, L->stream);
         L->minmax.alloc(2, L->stream);
@@ -274,7 +279,10 @@ void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref
     k_mean_final<<<2, 256, 0, st>>>(L->mpart.p, nb, L->N, L->means.p);
     count_launch(2);
     launch_prefilter(L->coef.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
-    launch_pad_mirror(L->coef.p, L->coef_pad.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
+    if (L->d.dim == 2)
+        launch_pad_mirror(L->coef.p, L->coef_pad.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
+    else
+        launch_brick_pairs(L->coef.p, L->brick.p, L->n[0], L->n[1], L->n[2], st);
     check_launch("set_images kernels");
     L->images_set = true;
 }
@@ -494,8 +502,8 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
                     tile_z > 0 ? tile_z : lvl->tile[2]};
         if (lvl->d.dim == 2) t[2] = 1;
         if (!tile_supported(lvl->d.dim, t[0], t[1], t[2]))
-            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x8, 32x8x4, 32x4x4, 64x4x4, "
-                                        "64x8x4, 32x16x4, 32x16x8; 2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
+            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x16, 32x8x8, 32x8x4; "
+                                        "2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
         bool changed = false;
         for (int k = 0; k < 3; ++k)
             if (t[k] != lvl->tile[k]) {

@@ -336,6 +336,8 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         sm_adj = std::max(sm_adj, split_smem(a, 1));
         has_pen |= a.has_penalty;
     }
+    if (std::max(sm_warp, sm_adj) > 200 * 1024)
+        throw std::invalid_argument("coefficient spacing too small for the batched tile shape");
     DevBuf<EvalArgs> d_args;
     DevBuf<PairVec> d_vecs;
     DevBuf<MinState> d_states;
@@ -356,8 +358,8 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
                                 d_active.p, sm_warp, 0, st))
             throw std::invalid_argument("tile shape not compiled in");
-        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()), d_active.p,
-                           sm_adj, 1, st);
+        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
+                           d_active.p, sm_adj, 1, st);
         launch_gather_batch(dim, d_args.p, d_gitems.p, int(gitems.size()), d_active.p, d_nblocks.p, has_pen, st);
         k_min_update<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
         count_launch(2);
@@ -474,7 +476,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             cudaStream_t s;
             ~StreamGuard() { cudaStreamDestroy(s); }
         } guard{st};
-        int tile[3] = {32, 8, 8};
+        int tile[3] = {32, 8, 16};
         if (dim == 2) {
             tile[1] = 16;
             tile[2] = 1;

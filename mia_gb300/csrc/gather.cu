@@ -203,30 +203,29 @@ __global__ void __launch_bounds__(GT) k_gather_batch(const EvalArgs *__restrict_
 void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int nitems, const int *active,
                          const int *nblocks, int has_penalty, cudaStream_t st)
 {
+    (void)has_penalty;
     if (dim == 3) {
-        const size_t sm = (has_penalty ? 9 * 9 * 9 * 6 : 0) * sizeof(float);
-        k_gather_batch<3><<<nitems, GT, sm, st>>>(args, items, active, nblocks);
-    } else {
-        k_gather_batch<2><<<nitems, GT, 0, st>>>(args, items, active, nblocks);
+        launch_gather3_batch(args, items, nitems, active, nblocks, st);
+        return;
     }
+    k_gather_batch<2><<<nitems, GT, 0, st>>>(args, items, active, nblocks);
     count_launch();
 }
 
 int gather_blocks(const EvalArgs &a)
 {
-    const size_t ncoef = size_t(a.nc[0]) * a.nc[1] * (a.dim == 3 ? a.nc[2] : 1);
+    if (a.dim == 3) return gather3_blocks(a);
+    const size_t ncoef = size_t(a.nc[0]) * a.nc[1];
     return int((ncoef + GC - 1) / GC);
 }
 
 void launch_gather_mode(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st)
 {
-    const int nb = gather_blocks(a);
     if (a.dim == 3) {
-        const size_t sm = (a.has_penalty ? 9 * 9 * 9 * 6 : 0) * sizeof(float);
-        k_gather_b<3><<<nb, GT, sm, st>>>(a, with_gradient, dense);
-    } else {
-        k_gather_b<2><<<nb, GT, 0, st>>>(a, with_gradient, dense);
+        launch_gather3(a, with_gradient, dense, st);
+        return;
     }
+    k_gather_b<2><<<gather_blocks(a), GT, 0, st>>>(a, with_gradient, dense);
     count_launch();
 }
 

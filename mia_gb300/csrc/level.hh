@@ -134,10 +134,11 @@ struct mgr_level {
     int n[3] = {1, 1, 1}, nc[3] = {1, 1, 1};
     size_t N = 0, ncoef = 0, nparams = 0;
     int path = MGR_PATH_SPLIT;
-    int tile[3] = {32, 8, 8};
+    int tile[3] = {32, 8, 16};
     AxisDev ax[3];
     DevBuf<unsigned char> axis_tables;   // the packed AxisDev tables
     DevBuf<float> coef, coef_pad, ref, warped, minmax, partial, ptable, pen_val;
+    DevBuf<float2> brick;
     DevBuf<float2> mmpart;
     DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means, mpart;
     DevBuf<unsigned int> counters;
@@ -171,6 +172,9 @@ struct mgr_level {
         a.coef_img = coef.p;
         a.coef_pad = coef_pad.p;
         a.pad_rows = n[1] + 2 * PAD_H;
+        a.brick = brick.p;
+        a.bnx = brick_count(n[0], BRK_CX);
+        a.bny = brick_count(n[1], BRK_CY);
         a.ref = ref.p;
         a.warped = warped.p;
         a.minmax = minmax.p;
@@ -198,6 +202,26 @@ struct mgr_level {
         a.grad_penalty = nullptr;
         a.costs = costs.p;
         return a;
+    }
+
+    // 3D: the deepest z tile (16, 8, 4) whose warp and adjoint blocks fit in
+    // 64 KiB of shared memory (small coefficient spacings widen the
+    // footprints), keeping several blocks resident per SM
+    void choose_tile3()
+    {
+        static const int tzs[3] = {16, 8, 4};
+        for (int k = 0; k < 3; ++k) {
+            tile[0] = 32;
+            tile[1] = 8;
+            tile[2] = tzs[k];
+            AxisHost hx, hy, hz;
+            build_axis(hx, n[0], nc[0], tile[0]);
+            build_axis(hy, n[1], nc[1], tile[1]);
+            build_axis(hz, n[2], nc[2], tile[2]);
+            const size_t w = size_t(3) * hz.fc * hy.fc * (hx.fc + 32) * sizeof(float);
+            const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
+            if (std::max(w, adj) <= 64 * 1024) return;
+        }
     }
 
     void build_tables()

@@ -19,6 +19,9 @@ void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t 
 void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st);
 // the padded image's size in floats
 size_t pad_floats(int dim, int nx, int ny, int nz);
+// 3D bricked pair copy (mgr_common.cuh) and its size in float2
+void launch_brick_pairs(const float *img, float2 *out, int nx, int ny, int nz, cudaStream_t st);
+size_t brick_pairs(int nx, int ny, int nz);
 void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
                    float *out, cudaStream_t st);
 
@@ -29,8 +32,10 @@ struct EvalArgs {
     int nc[3];             // coefficient grid
     Axis ax[3];            // per-axis tables (ax[2] unused in 2D)
     const float *coef_img; // prefiltered moving image
-    const float *coef_pad; // the same with a mirror halo of PAD_H voxels (3D: all axes, 2D: x and y)
+    const float *coef_pad; // 2D: the same with a mirror halo of PAD_H voxels
     int pad_rows;          // rows per plane of coef_pad (ny + 2 PAD_H); the row pitch is pad_pitch(nx)
+    const float2 *brick;   // 3D: bricked pair copy (mgr_common.cuh)
+    int bnx, bny;          // bricks along x and y
     const float *ref;      // reference image
     float *warped;         // warped moving image (N)
     const float *minmax;   // device {min, max} clamp bounds
@@ -81,6 +86,19 @@ bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, c
                         const int *active, size_t smem, int which, cudaStream_t st);
 void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int nitems, const int *active,
                          const int *nblocks, int has_penalty, cudaStream_t st);
+
+// 3D split path (split3.cu): tiles of 32 x 8 x tz voxels, z-walking threads
+bool tile_supported3(int tx, int ty, int tz);
+size_t split3_smem(const EvalArgs &a, int which);
+void launch_warp3(const EvalArgs &a, cudaStream_t st);
+void launch_adjoint3(const EvalArgs &a, cudaStream_t st);
+int gather3_blocks(const EvalArgs &a);
+void launch_gather3(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st);
+void prepare_split3_batch(int tz, size_t sm_warp, size_t sm_adj);
+void launch_split3_batch(int tz, const EvalArgs *args, const int2 *items, int nitems, const int *active, size_t sm,
+                         int which, cudaStream_t st);
+void launch_gather3_batch(const EvalArgs *args, const int2 *items, int nitems, const int *active, const int *nblocks,
+                          cudaStream_t st);
 
 // standalone pieces for tests and the plain path
 void launch_force(const EvalArgs &a, float *force, cudaStream_t st);       // force field from `warped`

@@ -171,6 +171,34 @@ __global__ void k_pad_mirror(const float *__restrict__ img, float *__restrict__ 
     }
 }
 
+// bricked pair copy (layout in mgr_common.cuh), one float2 per thread
+__global__ void k_brick_pairs(const float *__restrict__ img, float2 *__restrict__ out, int nx, int ny, int nz,
+                              int nbx, int nby, size_t total)
+{
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const size_t b = i / BRK_N;
+        const int e = int(i - b * BRK_N);
+        const int lx = e % BRK_X, r = e / BRK_X, ly = r % BRK_Y, lz = r / BRK_Y;
+        const int bx = int(b % nbx), by = int((b / nbx) % nby), bz = int(b / (size_t(nbx) * nby));
+        const int x = bx * BRK_CX + lx - BRK_H, y = by * BRK_CY + ly - BRK_H, z = bz * BRK_CZ + lz - BRK_H;
+        const float *row = img + (size_t(mirror_fold(z, nz)) * ny + mirror_fold(y, ny)) * nx;
+        out[i] = make_float2(row[mirror_fold(x, nx)], row[mirror_fold(x + 1, nx)]);
+    }
+}
+
+size_t brick_pairs(int nx, int ny, int nz)
+{
+    return size_t(brick_count(nx, BRK_CX)) * brick_count(ny, BRK_CY) * brick_count(nz, BRK_CZ) * BRK_N;
+}
+
+void launch_brick_pairs(const float *img, float2 *out, int nx, int ny, int nz, cudaStream_t st)
+{
+    const size_t total = brick_pairs(nx, ny, nz);
+    const int nb = int(std::min<size_t>(8192, (total + 255) / 256));
+    k_brick_pairs<<<nb, 256, 0, st>>>(img, out, nx, ny, nz, brick_count(nx, BRK_CX), brick_count(ny, BRK_CY), total);
+    count_launch();
+}
+
 size_t pad_floats(int dim, int nx, int ny, int nz)
 {
     const int planes = dim == 3 ? nz + 2 * PAD_H : 1;

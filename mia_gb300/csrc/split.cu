@@ -559,48 +559,38 @@ static void launch_tile(const EvalArgs &a, int which, cudaStream_t st)
     count_launch();
 }
 
-// the tile shapes compiled in (tile_supported() must match)
+// the 2D tile shapes compiled in (tile_supported() must match); 3D runs
+// the z-walking kernels of split3.cu
 static bool dispatch(const EvalArgs &a, int which, cudaStream_t st)
 {
-    const int tx = a.ax[0].t, ty = a.ax[1].t, tz = a.dim == 3 ? a.ax[2].t : 1;
-#define MGR_TILE3(X_, Y_, Z_)                              \
-    if (a.dim == 3 && tx == X_ && ty == Y_ && tz == Z_) {  \
-        launch_tile<3, X_, Y_, Z_>(a, which, st);          \
-        return true;                                       \
+    if (a.dim == 3) {
+        if (which == 0)
+            launch_warp3(a, st);
+        else
+            launch_adjoint3(a, st);
+        return true;
     }
+    const int tx = a.ax[0].t, ty = a.ax[1].t;
 #define MGR_TILE2(X_, Y_)                                  \
-    if (a.dim == 2 && tx == X_ && ty == Y_) {              \
+    if (tx == X_ && ty == Y_) {                            \
         launch_tile<2, X_, Y_, 1>(a, which, st);           \
         return true;                                       \
     }
-    MGR_TILE3(32, 8, 8)
-    MGR_TILE3(32, 8, 4)
-    MGR_TILE3(32, 4, 4)
-    MGR_TILE3(64, 4, 4)
-    MGR_TILE3(64, 8, 4)
-    MGR_TILE3(32, 16, 4)
-    MGR_TILE3(32, 16, 8)
     MGR_TILE2(32, 8)
     MGR_TILE2(32, 16)
     MGR_TILE2(64, 8)
     MGR_TILE2(64, 16)
     MGR_TILE2(32, 32)
-#undef MGR_TILE3
 #undef MGR_TILE2
     return false;
 }
 
 bool tile_supported(int dim, int tx, int ty, int tz)
 {
-    static const int t3[][3] = {{32, 8, 8}, {32, 8, 4}, {32, 4, 4}, {64, 4, 4}, {64, 8, 4}, {32, 16, 4}, {32, 16, 8}};
     static const int t2[][2] = {{32, 8}, {32, 16}, {64, 8}, {64, 16}, {32, 32}};
-    if (dim == 3) {
-        for (auto &t : t3)
-            if (t[0] == tx && t[1] == ty && t[2] == tz) return true;
-    } else {
-        for (auto &t : t2)
-            if (t[0] == tx && t[1] == ty) return true;
-    }
+    if (dim == 3) return tile_supported3(tx, ty, tz);
+    for (auto &t : t2)
+        if (t[0] == tx && t[1] == ty) return true;
     return false;
 }
 
@@ -616,6 +606,7 @@ void launch_adjoint(const EvalArgs &a, cudaStream_t st)
 
 size_t split_smem(const EvalArgs &a, int which)
 {
+    if (a.dim == 3) return split3_smem(a, which);
     return which == 0 ? warp_smem(a) : adjoint_smem(a);
 }
 
@@ -639,52 +630,38 @@ static void prepare_batch_tile(size_t sm_warp, size_t sm_adj)
 
 void prepare_split_batch(int dim, int tx, int ty, int tz, size_t sm_warp, size_t sm_adj)
 {
-#define MGR_PTILE3(X_, Y_, Z_) \
-    if (dim == 3 && tx == X_ && ty == Y_ && tz == Z_) prepare_batch_tile<3, X_, Y_, Z_>(sm_warp, sm_adj);
+    if (dim == 3) {
+        prepare_split3_batch(tz, sm_warp, sm_adj);
+        return;
+    }
 #define MGR_PTILE2(X_, Y_) \
-    if (dim == 2 && tx == X_ && ty == Y_) prepare_batch_tile<2, X_, Y_, 1>(sm_warp, sm_adj);
-    MGR_PTILE3(32, 8, 8)
-    MGR_PTILE3(32, 8, 4)
-    MGR_PTILE3(32, 4, 4)
-    MGR_PTILE3(64, 4, 4)
-    MGR_PTILE3(64, 8, 4)
-    MGR_PTILE3(32, 16, 4)
-    MGR_PTILE3(32, 16, 8)
+    if (tx == X_ && ty == Y_) prepare_batch_tile<2, X_, Y_, 1>(sm_warp, sm_adj);
     MGR_PTILE2(32, 8)
     MGR_PTILE2(32, 16)
     MGR_PTILE2(64, 8)
     MGR_PTILE2(64, 16)
     MGR_PTILE2(32, 32)
-#undef MGR_PTILE3
 #undef MGR_PTILE2
 }
 
 bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, const int2 *items, int nitems,
                         const int *active, size_t sm, int which, cudaStream_t st)
 {
-#define MGR_BTILE3(X_, Y_, Z_)                                                  \
-    if (dim == 3 && tx == X_ && ty == Y_ && tz == Z_) {                         \
-        launch_batch_tile<3, X_, Y_, Z_>(args, items, nitems, active, sm, which, st); \
-        return true;                                                            \
+    if (dim == 3) {
+        if (!tile_supported3(tx, ty, tz)) return false;
+        launch_split3_batch(tz, args, items, nitems, active, sm, which, st);
+        return true;
     }
 #define MGR_BTILE2(X_, Y_)                                                      \
-    if (dim == 2 && tx == X_ && ty == Y_) {                                     \
+    if (tx == X_ && ty == Y_) {                                                 \
         launch_batch_tile<2, X_, Y_, 1>(args, items, nitems, active, sm, which, st); \
         return true;                                                            \
     }
-    MGR_BTILE3(32, 8, 8)
-    MGR_BTILE3(32, 8, 4)
-    MGR_BTILE3(32, 4, 4)
-    MGR_BTILE3(64, 4, 4)
-    MGR_BTILE3(64, 8, 4)
-    MGR_BTILE3(32, 16, 4)
-    MGR_BTILE3(32, 16, 8)
     MGR_BTILE2(32, 8)
     MGR_BTILE2(32, 16)
     MGR_BTILE2(64, 8)
     MGR_BTILE2(64, 16)
     MGR_BTILE2(32, 32)
-#undef MGR_BTILE3
 #undef MGR_BTILE2
     return false;
 }
