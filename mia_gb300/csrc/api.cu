@@ -180,15 +180,14 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
             L->own_stream = true;
         }
         L->coef.alloc(L->N, L->stream);
-        if (d.dim == 2)
-            L->coef_pad.alloc(pad_floats(d.dim, L->n[0], L->n[1], L->n[2]), L->stream);
-        else
-            L->brick.alloc(brick_pairs(L->n[0], L->n[1], L->n[2]), L->stream);
+        L->coef_pad.alloc(pad_floats(d.dim, L->n[0], L->n[1], L->n[2]), L->stream);
+        if (d.dim == 3) L->has_tmap = encode_pad_tmap(&L->tmap, L->coef_pad.p, L->n[0], L->n[1], L->n[2]);
         L->ref.alloc(L->N, L->stream);
         L->warped.alloc(L->N, L->stream);
         L->minmax.alloc(2, L->stream);
         L->mmpart.alloc(1024, L->stream);
         L->params.alloc(L->nparams, L->stream);
+        if (d.dim == 3) L->params_f.alloc(L->nparams, L->stream);
         L->grad_total.alloc(L->nparams, L->stream);
         L->scalars.alloc(SC_NSLOTS, L->stream);
         L->costs.alloc(2, L->stream);
@@ -279,10 +278,7 @@ void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref
     k_mean_final<<<2, 256, 0, st>>>(L->mpart.p, nb, L->N, L->means.p);
     count_launch(2);
     launch_prefilter(L->coef.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
-    if (L->d.dim == 2)
-        launch_pad_mirror(L->coef.p, L->coef_pad.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
-    else
-        launch_brick_pairs(L->coef.p, L->brick.p, L->n[0], L->n[1], L->n[2], st);
+    launch_pad_mirror(L->coef.p, L->coef_pad.p, L->d.dim, L->n[0], L->n[1], L->n[2], st);
     check_launch("set_images kernels");
     L->images_set = true;
 }

@@ -307,7 +307,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     std::vector<MinState> states(np);
     std::vector<int2> titems, gitems;
     std::vector<int> nblocks(np);
-    size_t sm_warp = 0, sm_adj = 0;
+    size_t sm_warp = 0, sm_adj = 0, max_params = 0;
     int has_pen = 0;
     for (int k = 0; k < np; ++k) {
         PairRun &r = *pairs[members[k]];
@@ -335,6 +335,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         sm_warp = std::max(sm_warp, split_smem(a, 0));
         sm_adj = std::max(sm_adj, split_smem(a, 1));
         has_pen |= a.has_penalty;
+        max_params = std::max(max_params, n);
     }
     if (std::max(sm_warp, sm_adj) > 200 * 1024)
         throw std::invalid_argument("coefficient spacing too small for the batched tile shape");
@@ -355,6 +356,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
 
     auto step = [&]() {
         k_min_propose<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
+        if (dim == 3) launch_params_f32_batch(d_args.p, d_active.p, np, max_params, st);
         if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
                                 d_active.p, sm_warp, 0, st))
             throw std::invalid_argument("tile shape not compiled in");
@@ -369,7 +371,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     // kernel attributes are set outside the capture
     prepare_split_batch(dim, tile[0], tile[1], tile[2], sm_warp, sm_adj);
     cudaGraphExec_t exec = nullptr;
-    const unsigned kernels_per_chunk = unsigned(chunk) * 5 + 1;
+    const unsigned kernels_per_chunk = unsigned(chunk) * (dim == 3 ? 6 : 5) + 1;
     tr_setup.stop();
     if (use_graphs) {
         TraceScope tr("batch: graph capture", st);

@@ -267,6 +267,7 @@ void launch_translate(const EvalArgs &a, const float *force, double *grad, float
 void launch_plain_eval(const EvalArgs &a, float *grid, float *force, float *tmp1, float *tmp2,
                        cudaStream_t st)
 {
+    if (a.dim == 3) launch_params_f32(a, st);   // read by the gather's penalty
     const int nx = a.n[0], ny = a.n[1], nz = a.dim == 3 ? a.n[2] : 1;
     const size_t N = size_t(nx) * ny * nz;
     const int nb = int((N + 255) / 256);

@@ -79,7 +79,7 @@ struct DevBuf {
 // host blob and uploaded with one copy; `off` are byte offsets into it
 struct AxisDev {
     AxisHost h;
-    size_t off[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // fs, as, rows, ftile0, atile0, gtile, fw, aw
+    size_t off[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // fs, as, rows, ftile0, atile0, gtile, fw, aw, glist, glen
     const unsigned char *base = nullptr;
 
     template <class T>
@@ -100,6 +100,8 @@ struct AxisDev {
         off[5] = pack(blob, h.gtile);
         off[6] = pack(blob, h.fw);
         off[7] = pack(blob, h.aw);
+        off[8] = pack(blob, h.glist);
+        off[9] = pack(blob, h.glen);
     }
     Axis view() const
     {
@@ -112,6 +114,8 @@ struct AxisDev {
         a.gtile = reinterpret_cast<const int2 *>(base + off[5]);
         a.fw = reinterpret_cast<const float4 *>(base + off[6]);
         a.aw = reinterpret_cast<const float4 *>(base + off[7]);
+        a.glist = reinterpret_cast<const int *>(base + off[8]);
+        a.glen = reinterpret_cast<const int *>(base + off[9]);
         a.n = h.n;
         a.nc = h.nc;
         a.t = h.t;
@@ -137,13 +141,14 @@ struct mgr_level {
     int tile[3] = {32, 8, 16};
     AxisDev ax[3];
     DevBuf<unsigned char> axis_tables;   // the packed AxisDev tables
-    DevBuf<float> coef, coef_pad, ref, warped, minmax, partial, ptable, pen_val;
-    DevBuf<float2> brick;
+    DevBuf<float> coef, coef_pad, ref, warped, minmax, partial, ptable, pen_val, params_f;
     DevBuf<float2> mmpart;
     DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means, mpart;
     DevBuf<unsigned int> counters;
     DevBuf<int> pen_rowptr, pen_col;
     DevBuf<float> grid, force, tmp1, tmp2;   // plain path and standalone force/translate
+    CUtensorMap tmap{};     // 3D: tensor map of coef_pad
+    bool has_tmap = false;
     int slot = 0;
     bool images_set = false;
     bool tables_valid = false;
@@ -163,6 +168,8 @@ struct mgr_level {
     EvalArgs args() const
     {
         EvalArgs a{};
+        a.tmap = tmap;
+        a.has_tmap = has_tmap;
         a.dim = d.dim;
         for (int k = 0; k < 3; ++k) {
             a.n[k] = n[k];
@@ -172,13 +179,11 @@ struct mgr_level {
         a.coef_img = coef.p;
         a.coef_pad = coef_pad.p;
         a.pad_rows = n[1] + 2 * PAD_H;
-        a.brick = brick.p;
-        a.bnx = brick_count(n[0], BRK_CX);
-        a.bny = brick_count(n[1], BRK_CY);
         a.ref = ref.p;
         a.warped = warped.p;
         a.minmax = minmax.p;
         a.params = params.p;
+        a.params_f = params_f.p;
         a.cost = d.cost;
         a.ssd_norm = d.ssd_norm;
         a.cost_weight = d.cost_weight;
@@ -204,9 +209,9 @@ struct mgr_level {
         return a;
     }
 
-    // 3D: the deepest z tile (16, 8, 4) whose warp and adjoint blocks fit in
-    // 64 KiB of shared memory (small coefficient spacings widen the
-    // footprints), keeping several blocks resident per SM
+    // 3D: the deepest z tile (16, 8, 4) whose warp block fits three to an SM
+    // and whose adjoint block fits in 64 KiB of shared memory (small
+    // coefficient spacings widen the footprints)
     void choose_tile3()
     {
         static const int tzs[3] = {16, 8, 4};
@@ -218,9 +223,9 @@ struct mgr_level {
             build_axis(hx, n[0], nc[0], tile[0]);
             build_axis(hy, n[1], nc[1], tile[1]);
             build_axis(hz, n[2], nc[2], tile[2]);
-            const size_t w = size_t(3) * hz.fc * hy.fc * (hx.fc + 32) * sizeof(float);
+            const size_t w = (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(12) * 16 * 64) * sizeof(float);
             const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
-            if (std::max(w, adj) <= 64 * 1024) return;
+            if (w <= 74 * 1024 && adj <= 64 * 1024) return;
         }
     }
 
@@ -228,10 +233,31 @@ struct mgr_level {
     {
         const int D = d.dim;
         std::vector<unsigned char> blob;
-        for (int k = 0; k < D; ++k) {
-            build_axis(ax[k].h, n[k], nc[k], tile[k]);
-            ax[k].pack_all(blob);
+        for (int k = 0; k < D; ++k) build_axis(ax[k].h, n[k], nc[k], tile[k]);
+        if (D == 3) {
+            // per axis and coefficient: the partial-slot offset parts of the
+            // tiles that hold it, slot entry (tx, ty, tz) of coefficient
+            // (cx, cy, cz) being at glist_x + glist_y + glist_z
+            const int sl = D * ax[0].h.ac * ax[1].h.ac * ax[2].h.ac;
+            const long long total = (long long)ax[0].h.nt * ax[1].h.nt * ax[2].h.nt * sl;
+            const long long ts[3] = {sl, (long long)ax[0].h.nt * sl, (long long)ax[0].h.nt * ax[1].h.nt * sl};
+            const long long ls[3] = {D, (long long)ax[0].h.ac * D, (long long)ax[0].h.ac * ax[1].h.ac * D};
+            for (int k = 0; k < 3; ++k) {
+                AxisHost &h = ax[k].h;
+                h.glist.assign(size_t(h.nc) * GATHER_LMAX, 0);
+                h.glen.assign(h.nc, -1);
+                for (int c = 0; c < h.nc; ++c) {
+                    const int lo = h.gtile[size_t(c) * 2], hi = h.gtile[size_t(c) * 2 + 1];
+                    const int cnt = std::max(hi - lo + 1, 0);
+                    if (cnt > GATHER_LMAX || total >= (1LL << 31)) continue;
+                    for (int j = 0; j < cnt; ++j)
+                        h.glist[size_t(c) * GATHER_LMAX + j] =
+                            int((lo + j) * ts[k] + (c - h.atile0[lo + j]) * ls[k]);
+                    h.glen[c] = cnt;
+                }
+            }
         }
+        for (int k = 0; k < D; ++k) ax[k].pack_all(blob);
         // a fresh buffer: kernels queued earlier may still read the old one
         axis_tables.release();
         axis_tables.upload(blob, stream);

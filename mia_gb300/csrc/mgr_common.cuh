@@ -68,26 +68,6 @@ __host__ __device__ constexpr int stage_floats(int dim, int tx, int ty, int tz)
     return stage_bx(tx) * stage_by(ty) * stage_bz(dim, tz);
 }
 
-// Bricked pair copy of a 3D prefiltered image, the tap source of the 3D
-// warp kernel.  The image is mirror-padded by BRK_H voxels on every side
-// (padded coordinate g = i + BRK_H) and cut into bricks whose cores hold
-// BRK_CX x BRK_CY x BRK_CZ tap start positions; a brick also stores the
-// 3 (y, z) or 2 (x, in pairs) positions past its core, so the 4 x 4 x 4 taps
-// of any start position lie in one brick at compile-time pitches.  Element
-// (lx, ly, lz) of brick (bx, by, bz) holds the pair F(gx - H), F(gx + 1 - H)
-// at gx = bx CX + lx (and F at gy, gz likewise), mirror-folded.
-constexpr int BRK_H = 8;
-constexpr int BRK_CX = 32, BRK_CY = 16, BRK_CZ = 16;
-constexpr int BRK_X = BRK_CX + 2, BRK_Y = BRK_CY + 3, BRK_Z = BRK_CZ + 3;
-constexpr int BRK_N = BRK_X * BRK_Y * BRK_Z;   // float2 per brick
-
-// bricks along an axis of n voxels with core c: tap starts g in
-// [0, n + 2 BRK_H - 4]
-__host__ __device__ inline int brick_count(int n, int core)
-{
-    return (n + 2 * BRK_H - 4) / core + 1;
-}
-
 // Mirror boundary index folding with period 2w-2
 // (mia/core/splinebc/bc.cc:52-64).
 __device__ __forceinline__ int mirror_fold(int i, int w)
@@ -285,6 +265,8 @@ struct Axis {
     const int *ftile0;  // per tile: first coefficient of the forward footprint
     const int *atile0;  // per tile: first coefficient of the adjoint footprint
     const int2 *gtile;  // per coefficient: tiles [lo, hi] whose adjoint footprint holds it
+    const int *glist;   // 3D, per coefficient: GATHER_LMAX offsets into the partial slots, this axis' part
+    const int *glen;    // 3D, per coefficient: entries of glist (-1: longer than GATHER_LMAX)
     int n;              // voxels
     int nc;             // coefficients
     int t;              // tile length (voxels)
@@ -292,6 +274,10 @@ struct Axis {
     int fc;             // forward footprint length (max over tiles)
     int ac;             // adjoint footprint length (max over tiles)
 };
+
+// longest per-axis list of tiles whose adjoint footprint holds a coefficient
+// that the 3D gather reads from the tables (longer lists take a slower path)
+constexpr int GATHER_LMAX = 24;
 
 // scalars written by the cost finalisation (double[16])
 enum {

@@ -1,6 +1,7 @@
 // mgr_kernels.hh — host-side launchers of the libmgr kernels.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -19,27 +20,30 @@ void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t 
 void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st);
 // the padded image's size in floats
 size_t pad_floats(int dim, int nx, int ny, int nz);
-// 3D bricked pair copy (mgr_common.cuh) and its size in float2
-void launch_brick_pairs(const float *img, float2 *out, int nx, int ny, int nz, cudaStream_t st);
-size_t brick_pairs(int nx, int ny, int nz);
 void launch_minmax(const float *img, size_t n, float2 *part, int nblocks, unsigned int *counter,
                    float *out, cudaStream_t st);
 
+// 3D: tensor map of the padded copy (box 64 x 16 x 1 floats, the
+// warp kernel's shared-memory ring planes); false if the driver offers no
+// tensor-map encoder (the kernel then reads its taps from global memory)
+bool encode_pad_tmap(CUtensorMap *map, const float *pad, int nx, int ny, int nz);
+
 // ---- the evaluation pipeline ----------------------------------------
 struct EvalArgs {
+    CUtensorMap tmap;      // 3D: encode_pad_tmap of coef_pad (first: 64-byte aligned)
+    int has_tmap;
     int dim;
     int n[3];              // image size
     int nc[3];             // coefficient grid
     Axis ax[3];            // per-axis tables (ax[2] unused in 2D)
     const float *coef_img; // prefiltered moving image
-    const float *coef_pad; // 2D: the same with a mirror halo of PAD_H voxels
+    const float *coef_pad; // the same with a mirror halo of PAD_H voxels (3D: all axes, 2D: x and y)
     int pad_rows;          // rows per plane of coef_pad (ny + 2 PAD_H); the row pitch is pad_pitch(nx)
-    const float2 *brick;   // 3D: bricked pair copy (mgr_common.cuh)
-    int bnx, bny;          // bricks along x and y
     const float *ref;      // reference image
     float *warped;         // warped moving image (N)
     const float *minmax;   // device {min, max} clamp bounds
     const double *params;  // spline parameters, interleaved, device
+    float *params_f;       // 3D: their float copy (launch_params_f32), read by the warp and gather kernels
     int cost;              // MGR_COST_SSD / NCC
     int ssd_norm;
     double cost_weight;
@@ -87,7 +91,11 @@ bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, c
 void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int nitems, const int *active,
                          const int *nblocks, int has_penalty, cudaStream_t st);
 
-// 3D split path (split3.cu): tiles of 32 x 8 x tz voxels, z-walking threads
+// 3D split path (split3.cu): tiles of 32 x 8 x tz voxels, z-walking threads;
+// launch_warp3 converts the parameters to float first (launch_params_f32)
+void launch_params_f32(const EvalArgs &a, cudaStream_t st);
+// batch: every active pair's parameters (grid sized by the largest pair)
+void launch_params_f32_batch(const EvalArgs *args, const int *active, int npairs, size_t max_params, cudaStream_t st);
 bool tile_supported3(int tx, int ty, int tz);
 size_t split3_smem(const EvalArgs &a, int which);
 void launch_warp3(const EvalArgs &a, cudaStream_t st);

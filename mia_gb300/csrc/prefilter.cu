@@ -5,6 +5,8 @@
 // (mia/core/boundary_conditions.cc:62-103) and CMirrorOnBoundary
 // (mia/core/splinebc/bc.cc:67-88): x lines, then y lines, then z lines, each
 // line filtered in double and stored back as float.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include "mgr_common.cuh"
 #include "mgr_kernels.hh"
@@ -171,32 +173,28 @@ __global__ void k_pad_mirror(const float *__restrict__ img, float *__restrict__ 
     }
 }
 
-// bricked pair copy (layout in mgr_common.cuh), one float2 per thread
-__global__ void k_brick_pairs(const float *__restrict__ img, float2 *__restrict__ out, int nx, int ny, int nz,
-                              int nbx, int nby, size_t total)
+bool encode_pad_tmap(CUtensorMap *map, const float *pad, int nx, int ny, int nz)
 {
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
-        const size_t b = i / BRK_N;
-        const int e = int(i - b * BRK_N);
-        const int lx = e % BRK_X, r = e / BRK_X, ly = r % BRK_Y, lz = r / BRK_Y;
-        const int bx = int(b % nbx), by = int((b / nbx) % nby), bz = int(b / (size_t(nbx) * nby));
-        const int x = bx * BRK_CX + lx - BRK_H, y = by * BRK_CY + ly - BRK_H, z = bz * BRK_CZ + lz - BRK_H;
-        const float *row = img + (size_t(mirror_fold(z, nz)) * ny + mirror_fold(y, ny)) * nx;
-        out[i] = make_float2(row[mirror_fold(x, nx)], row[mirror_fold(x + 1, nx)]);
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
     }
-}
-
-size_t brick_pairs(int nx, int ny, int nz)
-{
-    return size_t(brick_count(nx, BRK_CX)) * brick_count(ny, BRK_CY) * brick_count(nz, BRK_CZ) * BRK_N;
-}
-
-void launch_brick_pairs(const float *img, float2 *out, int nx, int ny, int nz, cudaStream_t st)
-{
-    const size_t total = brick_pairs(nx, ny, nz);
-    const int nb = int(std::min<size_t>(8192, (total + 255) / 256));
-    k_brick_pairs<<<nb, 256, 0, st>>>(img, out, nx, ny, nz, brick_count(nx, BRK_CX), brick_count(ny, BRK_CY), total);
-    count_launch();
+    if (!fn) return false;
+    const int P = pad_pitch(nx);
+    const cuuint64_t dims[3] = {cuuint64_t(P), cuuint64_t(ny + 2 * PAD_H), cuuint64_t(nz + 2 * PAD_H)};
+    const cuuint64_t strides[2] = {cuuint64_t(P) * 4, cuuint64_t(P) * (ny + 2 * PAD_H) * 4};
+    const cuuint32_t box[3] = {64, 16, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(pad), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 size_t pad_floats(int dim, int nx, int ny, int nz)

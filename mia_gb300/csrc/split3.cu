@@ -12,9 +12,12 @@
 //       needs in registers and slides them as z advances, giving u(x); the
 //       prefiltered moving image is sampled with the tricubic B-spline at
 //       x - u(x) (mia/3d/interpolator.cxx:250-287, mirror boundary, clamp
-//       to [min(0, min src), max src]) from a bricked, mirror-padded copy,
-//       so the interior needs no index folding and every tap address is an
-//       immediate offset; the warped image is written and
+//       to [min(0, min src), max src]); the taps are read from a ring of z
+//       planes in shared memory that bulk copies fill ahead of the walk from
+//       a mirror-padded copy (the box of a plane follows from the range of
+//       u over the tile), so the interior needs no index folding and the
+//       gather costs shared-memory wavefronts instead of L1 lines; the
+//       warped image is written and
 //       the SSD / NCC sums are accumulated; the last block finalises the
 //       cost.
 //   k_adjoint3<TZ>    central differences of the warped image (x neighbours
@@ -33,6 +36,8 @@
 //       parameters with a 3-node halo, the penalty weight and sign
 //       (mia/3d/splinetransformpenalty.cc:60-71) and the full-cost weight
 //       (mia/template/fullcost.cxx:37-45).
+#include <algorithm>
+
 #include "mgr_cost.cuh"
 
 namespace mgr {
@@ -44,59 +49,105 @@ constexpr int TX3 = 32;    // tile x (lanes)
 constexpr int TY3 = 8;     // tile y (warps)
 constexpr unsigned FULL = 0xffffffffu;
 
-// Packed (two lanes of a float2) cubic B-spline weights, the operations and
-// their order as bspline3_weights: the x and y weights of a sample point in
-// one pass.
-__device__ __forceinline__ void bspline3_weights2(float2 f, float2 w[4])
-{
-    const float2 one = make_float2(1.0f, 1.0f), neg = make_float2(-1.0f, -1.0f);
-    const float2 ob6 = make_float2(1.0f / 6.0f, 1.0f / 6.0f);
-    const float2 xm1 = __ffma2_rn(neg, f, one);
-    const float2 w0 = __fmul2_rn(__fmul2_rn(xm1, xm1), __fmul2_rn(xm1, ob6));
-    const float2 w3 = __fmul2_rn(__fmul2_rn(f, f), __fmul2_rn(f, ob6));
-    w[0] = w0;
-    w[3] = w3;
-    w[1] = __fadd2_rn(__ffma2_rn(neg, w0, __ffma2_rn(neg, w0, xm1)), w3);
-    w[2] = __fadd2_rn(__ffma2_rn(neg, w3, __ffma2_rn(neg, w3, f)), w0);
-}
-
-// Tricubic sample at (px, py, pz) from the bricked pair copy: the 4 x 4 x 4
-// taps of the start position lie in one brick at compile-time pitches (two
-// 8-byte loads per tap row, immediate offsets).  Each row's sum is kept as a
-// pair (even taps, odd taps) through the y and z contractions, in packed
-// FP32 FMAs, and the pair is added at the end.  Sample points whose taps
-// leave the padded box fold their indices on the unpadded image (sample3).
-__device__ __forceinline__ float taps3(const EvalArgs &a, float px, float py, float pz, float mn, float mx)
+// Tricubic sample at (px, py, pz) read from global memory: the taps come
+// from the mirror-padded copy coef_pad while they lie inside it, else the
+// indices are folded on the unpadded image (sample3).  Same weights and
+// summation order as sample3.  This is the path of voxels whose taps are
+// not in the shared-memory ring below.
+__device__ __noinline__ float taps3_global(const EvalArgs &a, float px, float py, float pz, float mn, float mx)
 {
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
     const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
-    const int gx = fx - 1 + BRK_H, gy = fy - 1 + BRK_H, gz = fz - 1 + BRK_H;
-    if (unsigned(gx) <= unsigned(nx + 2 * BRK_H - 4) && unsigned(gy) <= unsigned(ny + 2 * BRK_H - 4) &&
-        unsigned(gz) <= unsigned(nz + 2 * BRK_H - 4)) {
-        float2 wxy[4];
-        bspline3_weights2(make_float2(px - float(fx), py - float(fy)), wxy);
-        float wz[4];
+    const int sx = fx - 1, sy = fy - 1, sz = fz - 1;
+    constexpr int H = PAD_H;
+    if (sx >= -H && sx + 3 < nx + H && sy >= -H && sy + 3 < ny + H && sz >= -H && sz + 3 < nz + H) {
+        float wx[4], wy[4], wz[4];
+        bspline3_weights(px - float(fx), wx);
+        bspline3_weights(py - float(fy), wy);
         bspline3_weights(pz - float(fz), wz);
-        const int bi = ((gz / BRK_CZ) * a.bny + gy / BRK_CY) * a.bnx + gx / BRK_CX;
-        const float2 *__restrict__ b = a.brick + size_t(bi) * BRK_N +
-                                       ((gz % BRK_CZ) * BRK_Y + (gy % BRK_CY)) * BRK_X + (gx % BRK_CX);
-        const float2 wx01 = make_float2(wxy[0].x, wxy[1].x), wx23 = make_float2(wxy[2].x, wxy[3].x);
-        float2 acc2 = make_float2(0.0f, 0.0f);
+        const int P = pad_pitch(nx);
+        const size_t PL = size_t(P) * a.pad_rows;
+        const float *__restrict__ b = a.coef_pad + (size_t(sz + H) * a.pad_rows + (sy + H)) * P + (sx + H);
+        float acc = 0.0f;
 #pragma unroll
         for (int kz = 0; kz < 4; ++kz) {
-            float2 s2 = make_float2(0.0f, 0.0f);
+            float ay = 0.0f;
 #pragma unroll
             for (int ky = 0; ky < 4; ++ky) {
-                const float2 *__restrict__ row = b + (kz * BRK_Y + ky) * BRK_X;
-                float2 r = __fmul2_rn(wx01, __ldg(row));
-                r = __ffma2_rn(wx23, __ldg(row + 2), r);
-                s2 = __ffma2_rn(make_float2(wxy[ky].y, wxy[ky].y), r, s2);
+                const float *__restrict__ row = b + kz * PL + ky * P;
+                const float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) +
+                                wx[3] * __ldg(row + 3);
+                ay += wy[ky] * r;
             }
-            acc2 = __ffma2_rn(make_float2(wz[kz], wz[kz]), s2, acc2);
+            acc += wz[kz] * ay;
         }
-        return clamp_ref(acc2.x + acc2.y, mn, mx);
+        return clamp_ref(acc, mn, mx);
     }
     return sample3(a.coef_img, nx, ny, nz, px, py, pz, mn, mx);
+}
+
+// Shared-memory ring of tap planes of the 3D warp kernel: RING_N planes of
+// RING_Y rows of RING_X floats (a row holds the x extent of a tile's taps
+// plus the alignment of the copies; its pitch is a multiple of the 32
+// banks, so a warp whose lanes straddle two rows or planes reads without
+// bank conflicts).  A tile whose taps do not fit (large variation of the
+// displacement over the tile) reads them from global memory instead.
+constexpr int RING_N = 12;
+constexpr int RING_Y = 16;
+constexpr int RING_X = 64;
+constexpr int RING_PLANE = RING_Y * RING_X;
+
+__device__ __forceinline__ int ring_slot(int k)
+{
+    return k % RING_N;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Bounded wait on phase `parity` of an mbarrier: false after the iteration
+// limit (the copy engine did not deliver), so that no wait is endless.
+__device__ __forceinline__ bool mbar_wait(unsigned mb, unsigned parity)
+{
+    for (int it = 0; it < (1 << 20); ++it) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(mb), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Tricubic sample from the ring: `row`/`col` locate the first tap inside a
+// plane and `slot0` is the ring slot of the first tap plane; the weights and
+// the summation order are those of sample3.
+__device__ __forceinline__ float taps3_ring(const float *ring, int slot0, int row, int col, float fx, float fy,
+                                           float fz, float mn, float mx)
+{
+    float wx[4], wy[4], wz[4];
+    bspline3_weights(fx, wx);
+    bspline3_weights(fy, wy);
+    bspline3_weights(fz, wz);
+    const float *base = ring + row * RING_X + col;
+    float acc = 0.0f;
+#pragma unroll
+    for (int kz = 0; kz < 4; ++kz) {
+        int sl = slot0 + kz;
+        sl = sl >= RING_N ? sl - RING_N : sl;
+        const float *pl = base + sl * RING_PLANE;
+        float ay = 0.0f;
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky) {
+            const float *r = pl + ky * RING_X;
+            ay += wy[ky] * (wx[0] * r[0] + wx[1] * r[1] + wx[2] * r[2] + wx[3] * r[3]);
+        }
+        acc += wz[kz] * ay;
+    }
+    return clamp_ref(acc, mn, mx);
 }
 
 }  // namespace
@@ -110,8 +161,12 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     extern __shared__ __align__(16) float sm3[];
     __shared__ double red[5 * (NT3 / 32)];
     __shared__ float wsum[5][NT3 / 32];
+    __shared__ float csc[2];   // NCC centres (converted once per block)
     __shared__ int zs[TZ];
     __shared__ float4 zw[TZ];
+    __shared__ float urng[NT3 / 32][6];   // per warp: footprint min / max per component
+    __shared__ int boxs[8];               // staged, xs, ylo, zbase, nplanes, span, w4, rows
+    __shared__ __align__(8) unsigned long long mbar[RING_N];
     __shared__ bool is_last;
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
@@ -135,43 +190,55 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         fwz = Z.fw[z];
     }
     const float mn = a.minmax[0], mxv = a.minmax[1];
-    const float ca = float(a.centers[0]), cb = float(a.centers[1]);
+    if (tid == 0) {
+        csc[0] = float(a.centers[0]);
+        csc[1] = float(a.centers[1]);
+    }
 
     float *C = sm3;                        // [3][FZ][FY][FX]
     float *Tx = C + 3 * FZ * FY * FX;      // [3][FZ][FY][32]
-    // coefficient footprint: rows (iz, iy) of 3 FX consecutive doubles
+    // [RING_N][RING_Y][RING_X]: the tensor copies want a 128-byte aligned
+    // destination, so the ring starts at the next 128-byte boundary of the
+    // shared window after Tx (the launch reserves the 128 bytes of slack)
+    float *ring;
+    {
+        const int off = 3 * FZ * FY * (FX + 32);
+        const unsigned ra = smem_u32(sm3 + off);
+        ring = sm3 + off + ((((ra + 127u) & ~127u) - ra) >> 2);
+    }
+    // coefficient footprint: rows (iz, iy) of 3 FX consecutive floats
     // (parameters are interleaved per node); each thread issues its loads
     // as one batch before storing
     {
         const int w3 = 3 * FX, nel = FZ * FY * w3;
-        auto src = [&](int e, int &dst) -> const double * {
+        auto src = [&](int e, int &dst) -> const float * {
             const int r = e / w3, j = e - r * w3;
             const int ix = j / 3, c = j - 3 * ix;
             const int iz = r / FY, iy = r - iz * FY;
             dst = (c * FZ * FY + r) * FX + ix;
             if (cx0 + ix >= ncx || cy0 + iy >= ncy || cz0 + iz >= ncz) return nullptr;
-            return a.params + ((size_t(cz0 + iz) * ncy + (cy0 + iy)) * ncx + cx0) * 3 + j;
+            return a.params_f + ((size_t(cz0 + iz) * ncy + (cy0 + iy)) * ncx + cx0) * 3 + j;
         };
         constexpr int K = 4;
-        double v[K];
+        float v[K];
         int dst[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int e = tid + k * NT3;
-            v[k] = 0.0;
+            v[k] = 0.0f;
             dst[k] = -1;
             if (e < nel) {
-                const double *p = src(e, dst[k]);
+                const float *p = src(e, dst[k]);
                 if (p) v[k] = *p;
             }
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)
-            if (dst[k] >= 0) C[dst[k]] = float(v[k]);
+            if (dst[k] >= 0) C[dst[k]] = v[k];
         for (int e = tid + K * NT3; e < nel; e += NT3) {
             int d;
-            const double *p = src(e, d);
-            C[d] = p ? float(*p) : 0.0f;
+            const float *p = src(e, d);
+            C[d] = p ? *p : 0.0f;
         }
     }
     if (tid < TZ) {
@@ -185,6 +252,11 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         for (int r = wy; r < 3 * FZ * FY; r += NT3 / 32) {
             const float *c = C + r * FX + sx;
             Tx[r * 32 + lane] = fwx.x * c[0] + fwx.y * c[1] + fwx.z * c[2] + fwx.w * c[3];
+        }
+        if (tid == 0) {
+            for (int k = 0; k < RING_N; ++k)
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[k])) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         }
     }
     __syncthreads();
@@ -200,17 +272,9 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
 #pragma unroll
         for (int m = 0; m < 4; ++m) q[c][m] = qat(c, m);
     int cur = 0;   // the window's first z coefficient (zs[0] == 0)
-
-    const bool inxy = (x0 + lane < nx) && (y0 + wy < ny);
-    const float px0 = float(x0 + lane), py0 = float(y0 + wy);
-    const size_t nxy = size_t(nx) * ny;
-    const size_t col = size_t(min(y0 + wy, ny - 1)) * nx + min(x0 + lane, nx - 1) + size_t(z0) * nxy;
-    float *wout = a.warped + col;
-    const float *rin = a.ref + col;
-    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    for (int t = 0; t < ez; ++t) {
+    auto advance = [&](int t) {   // the window moves to the coefficients of plane z0 + t (uniform)
         const int s = zs[t];
-        while (cur < s) {   // uniform over the block
+        while (cur < s) {
             ++cur;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -220,15 +284,160 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
                 q[c][3] = qat(c, cur + 3);
             }
         }
+    };
+    const bool inxy_t = (x0 + lane < nx) && (y0 + wy < ny);
+    {
+        // the range of u over the tile: along z, u is a combination of this
+        // thread's q values over the window range 0 .. zs[ez-1] + 3 with
+        // non-negative weights summing to 1 (to less than 1 on the last
+        // plane of the image, where 0 joins the range)
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        const int kend = zs[ez - 1] + 3;
+        for (int kz = 0; kz <= kend; ++kz)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float v = qat(c, kz);
+                lo[c] = fminf(lo[c], v);
+                hi[c] = fmaxf(hi[c], v);
+            }
+        const bool last_plane = z0 + ez == nz;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (last_plane) {
+                lo[c] = fminf(lo[c], 0.0f);
+                hi[c] = fmaxf(hi[c], 0.0f);
+            }
+            if (!inxy_t) {
+                lo[c] = 3.0e38f;
+                hi[c] = -3.0e38f;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[c] = fminf(lo[c], __shfl_xor_sync(FULL, lo[c], o));
+                hi[c] = fmaxf(hi[c], __shfl_xor_sync(FULL, hi[c], o));
+            }
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                urng[wy][c] = lo[c];
+                urng[wy][3 + c] = hi[c];
+            }
+    }
+    __syncthreads();
+    // tap box of the tile: x from xs (16-byte aligned in the padded rows),
+    // rows from ylo, planes zbase .. zbase + nplanes - 1 of which step t
+    // needs t .. t + span - 1; the ring is filled by bulk copies, one per
+    // row, completion counted on the plane's mbarrier
+    constexpr int H = PAD_H;
+    auto issue_plane = [&](int k) {   // thread 0: plane k of the box into its ring slot, one tensor copy
+        const int slot = ring_slot(k);
+        const unsigned mb = smem_u32(&mbar[slot]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb),
+                     "r"(unsigned(RING_PLANE) * 4u)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];\n" ::"r"(smem_u32(ring + slot * RING_PLANE)),
+            "l"(reinterpret_cast<unsigned long long>(&a.tmap)), "r"(boxs[1] + H), "r"(boxs[2] + H), "r"(boxs[3] + k + H),
+            "r"(mb)
+            : "memory");
+    };
+    if (tid == 0) {
+        float ulo[3], uhi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ulo[c] = urng[0][c];
+            uhi[c] = urng[0][3 + c];
+            for (int w = 1; w < NT3 / 32; ++w) {
+                ulo[c] = fminf(ulo[c], urng[w][c]);
+                uhi[c] = fmaxf(uhi[c], urng[w][3 + c]);
+            }
+        }
+        // taps of a voxel at p = v - u: floor(p) - 1 .. floor(p) + 2; the
+        // fixed-point floor may round p up to the next integer, one more
+        // row / column / plane on the upper side
+        const float big = 1.0e6f;
+        bool ok = a.has_tmap != 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ok = ok && fabsf(ulo[c]) < big && fabsf(uhi[c]) < big;
+        int xs = 0, xe = 0, ylo = 0, yhi = 0, dzl = 0, dzh = 0;
+        if (ok) {
+            const int xlo = int(floorf(float(x0) - uhi[0])) - 1;
+            xe = int(floorf(float(x0 + TX3 - 1) - ulo[0])) + 3;
+            xs = ((xlo + H) & ~3) - H;
+            ylo = int(floorf(float(y0) - uhi[1])) - 1;
+            yhi = int(floorf(float(y0 + ey - 1) - ulo[1])) + 3;
+            dzl = int(floorf(-uhi[2])) - 1;
+            dzh = int(floorf(-ulo[2])) + 3;
+            ok = xs >= -H && xe <= nx + H - 1 && xe - xs + 1 <= RING_X && ylo >= -H && yhi <= ny + H - 1 &&
+                 yhi - ylo + 1 <= RING_Y && z0 + dzl >= -H && z0 + ez - 1 + dzh <= nz + H - 1 &&
+                 dzh - dzl + 1 <= RING_N - 2;
+        }
+        boxs[0] = ok;
+        boxs[1] = xs;
+        boxs[2] = ylo;
+        boxs[3] = z0 + dzl;
+        boxs[4] = ez + dzh - dzl;
+        boxs[5] = dzh - dzl + 1;
+        boxs[6] = RING_X;
+        boxs[7] = yhi - ylo + 1;
+        if (ok)
+            for (int k = 0; k < min(boxs[4], RING_N); ++k) issue_plane(k);
+    }
+    __syncthreads();
+
+    const bool inxy = (x0 + lane < nx) && (y0 + wy < ny);
+    const float px0 = float(x0 + lane), py0 = float(y0 + wy);
+    const float ca = csc[0], cb = csc[1];
+    const size_t nxy = size_t(nx) * ny;
+    const size_t col = size_t(min(y0 + wy, ny - 1)) * nx + min(x0 + lane, nx - 1) + size_t(z0) * nxy;
+    float *wout = a.warped + col;
+    const float *rin = a.ref + col;
+    float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const bool staged = boxs[0] != 0;
+    const int bxs = boxs[1], bylo = boxs[2], bzbase = boxs[3], nplanes = boxs[4], span = boxs[5];
+    const int bw4 = boxs[6], brows = boxs[7];
+    bool ring_ok = staged;
+    int kwait = 0;      // planes below kwait have arrived
+    // the reference is streamed three planes ahead of its use (registers
+    // r0..r2), so the walk does not wait on its memory latency
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    if (inxy) {
+        r0 = __ldg(rin);
+        if (ez > 1) r1 = __ldg(rin + nxy);
+        if (ez > 2) r2 = __ldg(rin + 2 * nxy);
+    }
+    int issued = staged ? min(nplanes, RING_N) : 0;
+    for (int t = 0; t < ez; ++t) {
+        advance(t);
+        if (ring_ok) {
+            // the planes of this step (t .. t + span - 1) must have arrived
+            while (kwait <= t + span - 1) {
+                if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) {
+                    atomicOr(&a.counters[6], 1u);
+                    ring_ok = false;
+                    break;
+                }
+                ++kwait;
+            }
+        }
         const float4 wz = zw[t];
         float u[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) u[c] = wz.x * q[c][0] + wz.y * q[c][1] + wz.z * q[c][2] + wz.w * q[c][3];
         if (inxy) {
             const int z = z0 + t;
-            const float wv = taps3(a, px0 - u[0], py0 - u[1], float(z) - u[2], mn, mxv);
+            const float px = px0 - u[0], py = py0 - u[1], pz = float(z) - u[2];
+            const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
+            const int col = fx - 1 - bxs, row = fy - 1 - bylo, kk = fz - 1 - bzbase;
+            float wv;
+            if (ring_ok && col >= 0 && col + 3 < bw4 && row >= 0 && row + 3 < brows && kk >= t && kk + 3 <= t + span - 1)
+                wv = taps3_ring(ring, ring_slot(kk), row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
+            else
+                wv = taps3_global(a, px, py, pz, mn, mxv);
             *wout = wv;
-            const float b = __ldg(rin);
+            const float b = r0;
             if (a.cost == 0) {
                 const float d = wv - b;
                 acc[0] += d * d;
@@ -241,8 +450,28 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
                 acc[4] += da * db;
             }
         }
+        r0 = r1;
+        r1 = r2;
+        r2 = (inxy && t + 3 < ez) ? __ldg(rin + 3 * nxy) : 0.0f;
         wout += nxy;
         rin += nxy;
+        if (staged) {
+            // plane t is no longer needed: its slot takes plane t + RING_N
+            __syncthreads();
+            if (tid == 0 && ring_ok && t + RING_N < nplanes) {
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                issue_plane(t + RING_N);
+                ++issued;
+            }
+        }
+    }
+    if (staged && tid == 0) {
+        // copies still in flight (only after a wait gave up) are waited for
+        // before the block's shared memory is released
+        while (kwait < issued) {
+            if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) break;
+            ++kwait;
+        }
     }
     // tile sums: a float tree within each warp (5 levels), the warps' sums
     // added in double in a fixed order by thread 0 (FP64 is slow here, so
@@ -283,6 +512,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
 {
     extern __shared__ __align__(16) float sm3[];
     __shared__ int asx[TX3], asy[TY3], azs[TZ];
+    __shared__ float fsc[5];   // force constants (converted once per block)
     __shared__ float4 awx[TX3], awy[TY3], azw[TZ];
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
@@ -303,9 +533,10 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
     const size_t col = size_t(min(y, ny - 1)) * nx + min(x, nx - 1);
     const float *__restrict__ W = a.warped;
     const float *__restrict__ R = a.ref;
-    const double *sc = a.scalars;
-    const float k1 = float(sc[SC_K1]), k2 = float(sc[SC_K2]);
-    const float ma = float(sc[SC_MA]), mb = float(sc[SC_MB]), fscale = float(sc[SC_FSCALE]);
+    if (tid < 5) {
+        const int slot[5] = {SC_K1, SC_K2, SC_MA, SC_MB, SC_FSCALE};
+        fsc[tid] = float(a.scalars[slot[tid]]);
+    }
     const bool bx_in = x > 0 && x < nx - 1, by_in = y > 0 && y < ny - 1;
     // column pointers at the current plane
     const float *__restrict__ wc = W + size_t(z0) * nxy + col;
@@ -329,6 +560,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         azw[tid] = Z.aw[zz];
     }
     __syncthreads();
+    const float k1 = fsc[0], k2 = fsc[1], ma = fsc[2], mb = fsc[3], fscale = fsc[4];
 
     float acc[3][4];
 #pragma unroll
@@ -468,77 +700,68 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
 // ---------------------------------------------------------------------
 namespace {
 constexpr int GT3 = 256;
-constexpr int GB = 4;             // coefficients per block edge
-constexpr int GH = 3;             // stencil half width
-constexpr int GP = GB + 2 * GH;   // 10: halo tile edge
-constexpr int GPX = 12;           // padded row pitch (float4) of the halo tile
-constexpr int GLMAX = 24;         // longest staged per-axis tile list
+constexpr int GBX = 4, GBY = 4, GBZ = 2;   // coefficients per block: 32, lane = coefficient
+constexpr int GH = 3;                      // stencil half width
+constexpr int GPX = GBX + 2 * GH;          // 10: halo tile edges
+constexpr int GPY = GBY + 2 * GH;          // 10
+constexpr int GPZ = GBZ + 2 * GH;          // 8
+constexpr int GPP = 12;                    // padded row pitch (float4) of the halo tile
+constexpr int GSUB = GT3 / 32;             // 8 warps split each coefficient's work
+constexpr int GNQ = 12;                    // per-warp partials: 9 penalty products, 3 image sums
 }  // namespace
 
+// Block: 4 x 4 x 2 coefficients, one per lane; the 8 warps split the 49
+// (dz, dy) rows of the 7^3 divcurl stencil and the partial slots.  Loads are
+// issued in two batches: the tables, the parameters with a 3-node halo and
+// the penalty cells; then the partial slots, in flight while the stencil
+// is summed.
 __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradient, int image_from_dense, int blk,
                                              int nblk)
 {
-    __shared__ float4 Ps[GP * GP * GPX];
+    __shared__ float4 Ps[GPZ * GPY * GPP];
     __shared__ float4 Pt[343 * 2];
-    __shared__ float pacc[4][12][64];
-    __shared__ int gl[3][GB][GLMAX];   // per axis and coefficient of the block: slot offset part per tile
-    __shared__ int gn[3][GB];          // list lengths (-1: too long, use the tables directly)
-    __shared__ double red[GT3 / 32];
+    __shared__ float pacc[GSUB][GNQ][32];
+    __shared__ int gl[3][GBX][GATHER_LMAX];
+    __shared__ int gn[3][GBX];
+    __shared__ float wred[GSUB];
     __shared__ bool is_last;
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int ncx = a.nc[0], ncy = a.nc[1], ncz = a.nc[2];
-    const int nbx = (ncx + GB - 1) / GB, nby = (ncy + GB - 1) / GB;
+    const int nbx = (ncx + GBX - 1) / GBX, nby = (ncy + GBY - 1) / GBY;
     const int bxi = blk % nbx, byi = (blk / nbx) % nby, bzi = blk / (nbx * nby);
-    const int cx0 = bxi * GB, cy0 = byi * GB, cz0 = bzi * GB;
+    const int cx0 = bxi * GBX, cy0 = byi * GBY, cz0 = bzi * GBZ;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int sub = w >> 1;                   // 4 groups of 64 threads split the work of a coefficient
-    const int li = ((w & 1) << 5) | lane;     // coefficient of the block
-    const int lx = li & 3, ly = (li >> 2) & 3, lz = li >> 4;
+    const int lx = lane & 3, ly = (lane >> 2) & 3, lz = lane >> 4;
     const int cx = cx0 + lx, cy = cy0 + ly, cz = cz0 + lz;
     const bool valid = cx < ncx && cy < ncy && cz < ncz;
     const size_t i = valid ? (size_t(cz) * ncy + cy) * ncx + cx : 0;
+    const bool img = with_gradient && !image_from_dense;
 
-    // per axis a and coefficient c0 + k of the block: the tiles t whose
-    // adjoint footprint holds it and the part of the slot offset that
-    // depends on that axis (tile term, local term), so that the offset of
-    // slot entry (tx, ty, tz) is gl[0] + gl[1] + gl[2] (partial is indexed
-    // as ((tz nty + ty) ntx + tx) slot + ((lz acy + ly) acx + lx) 3)
-    if (with_gradient && !image_from_dense && tid < 3 * GB) {
-        const int ax = tid / GB, k = tid - ax * GB;
+    // batch 1: offset lists, parameters with halo, penalty cells
+    if (img && tid < 3 * GBX) {
+        const int ax = tid / GBX, k = tid - ax * GBX;
         const Axis &A = a.ax[ax];
         const int c = (ax == 0 ? cx0 : ax == 1 ? cy0 : cz0) + k;
         int cnt = 0;
-        if (c < A.nc) {
-            const int2 g = A.gtile[c];
-            cnt = max(g.y - g.x + 1, 0);
-            const long long nslots = (long long)X.nt * Y.nt * Z.nt * a.slot;
-            if (cnt > GLMAX || nslots >= (1LL << 31)) {
-                cnt = -1;
-            } else {
-                const int tstride = ax == 0 ? a.slot : ax == 1 ? X.nt * a.slot : X.nt * Y.nt * a.slot;
-                const int lstride = ax == 0 ? 3 : ax == 1 ? X.ac * 3 : X.ac * Y.ac * 3;
-                for (int j = 0; j < cnt; ++j) {
-                    const int t = g.x + j;
-                    gl[ax][k][j] = t * tstride + (c - A.atile0[t]) * lstride;
-                }
-            }
+        if (c < A.nc && (ax < 2 || k < GBZ)) {
+            cnt = A.glen[c];
+            for (int j = 0; j < cnt; ++j) gl[ax][k][j] = A.glist[size_t(c) * GATHER_LMAX + j];
         }
         gn[ax][k] = cnt;
     }
     if (a.has_penalty) {
-        // parameters of the block with a 3-node halo and the 7^3 cells of
-        // the penalty table, each thread's loads issued as one batch
-        constexpr int KP = (GP * GP * GP + GT3 - 1) / GT3;
-        double pv[KP][3];
+        constexpr int NH = GPX * GPY * GPZ;
+        constexpr int KP = (NH + GT3 - 1) / GT3;
+        float pv[KP][3];
 #pragma unroll
         for (int k = 0; k < KP; ++k) {
             const int e = tid + k * GT3;
-            pv[k][0] = pv[k][1] = pv[k][2] = 0.0;
-            if (e < GP * GP * GP) {
-                const int hx = e % GP, hy = (e / GP) % GP, hz = e / (GP * GP);
+            pv[k][0] = pv[k][1] = pv[k][2] = 0.0f;
+            if (e < NH) {
+                const int hx = e % GPX, hy = (e / GPX) % GPY, hz = e / (GPX * GPY);
                 const int gx = cx0 - GH + hx, gy = cy0 - GH + hy, gz = cz0 - GH + hz;
                 if (gx >= 0 && gx < ncx && gy >= 0 && gy < ncy && gz >= 0 && gz < ncz) {
-                    const double *p = a.params + ((size_t(gz) * ncy + gy) * ncx + gx) * 3;
+                    const float *p = a.params_f + ((size_t(gz) * ncy + gy) * ncx + gx) * 3;
                     pv[k][0] = p[0];
                     pv[k][1] = p[1];
                     pv[k][2] = p[2];
@@ -560,9 +783,9 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
 #pragma unroll
         for (int k = 0; k < KP; ++k) {
             const int e = tid + k * GT3;
-            if (e < GP * GP * GP) {
-                const int hx = e % GP, hy = (e / GP) % GP, hz = e / (GP * GP);
-                Ps[(hz * GP + hy) * GPX + hx] = make_float4(float(pv[k][0]), float(pv[k][1]), float(pv[k][2]), 0.0f);
+            if (e < NH) {
+                const int hx = e % GPX, hy = (e / GPX) % GPY, hz = e / (GPX * GPY);
+                Ps[(hz * GPY + hy) * GPP + hx] = make_float4(pv[k][0], pv[k][1], pv[k][2], 0.0f);
             }
         }
 #pragma unroll
@@ -575,13 +798,40 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
         }
     }
     __syncthreads();
+
+    // batch 2: this warp's share of the partial slots (entries k = w,
+    // w + 8, ...) of the lane's coefficient, issued before the stencil
+    constexpr int SMAX = 8;
+    float sv[SMAX][3];
+    int tot = 0, nX = 0, nY = 0, nZ = 0;
+    bool lists = false;
+    if (valid && img) {
+        nX = gn[0][lx];
+        nY = gn[1][ly];
+        nZ = gn[2][lz];
+        lists = nX >= 0 && nY >= 0 && nZ >= 0;
+        if (lists) tot = nX * nY * nZ;
+    }
+#pragma unroll
+    for (int u = 0; u < SMAX; ++u) {
+        const int k = w + GSUB * u;
+        sv[u][0] = sv[u][1] = sv[u][2] = 0.0f;
+        if (k < tot) {
+            const int jx = k % nX, r = k / nX;
+            const int jy = r % nY, jz = r / nY;
+            const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
+            sv[u][0] = p[0];
+            sv[u][1] = p[1];
+            sv[u][2] = p[2];
+        }
+    }
     // R0..R5, T0..T2: the nine products of the 3x3 cell with c_j, summed
     // over the 7^3 neighbours j = i - d (zero outside the grid)
     float R0 = 0, R1 = 0, R2 = 0, R3 = 0, R4 = 0, R5 = 0, T0 = 0, T1 = 0, T2 = 0;
     if (valid && a.has_penalty) {
-        for (int p = sub; p < 49; p += 4) {
+        for (int p = w; p < 49; p += GSUB) {
             const int dz = p / 7 - 3, dy = p % 7 - 3;
-            const float4 *prow = Ps + ((lz + GH - dz) * GP + (ly + GH - dy)) * GPX + (lx + GH);
+            const float4 *prow = Ps + ((lz + GH - dz) * GPY + (ly + GH - dy)) * GPP + (lx + GH);
             const float4 *trow = Pt + p * 14;
 #pragma unroll
             for (int k = 0; k < 7; ++k) {
@@ -599,112 +849,106 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             }
         }
     }
-    float S[3] = {0.0f, 0.0f, 0.0f};
-    if (valid && with_gradient && !image_from_dense) {
-        // the tiles whose slot holds this coefficient: a contiguous range per
-        // axis; the per-axis parts of the slot offsets come from the lists
-        // staged above, the rest is independent loads
-        const int nX = gn[0][lx], nY = gn[1][ly], nZ = gn[2][lz];
-        if (nX >= 0 && nY >= 0 && nZ >= 0) {
-            const int tot = nX * nY * nZ;
-            for (int k0 = sub; k0 < tot; k0 += 16) {
-                float v[4][3];
+    float S0 = 0.0f, S1 = 0.0f, S2 = 0.0f;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int k = k0 + 4 * u;
-                    v[u][0] = v[u][1] = v[u][2] = 0.0f;
-                    if (k < tot) {
-                        const int jx = k % nX, r = k / nX;
-                        const int jy = r % nY, jz = r / nY;
-                        const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
-                        v[u][0] = p[0];
-                        v[u][1] = p[1];
-                        v[u][2] = p[2];
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    S[0] += v[u][0];
-                    S[1] += v[u][1];
-                    S[2] += v[u][2];
-                }
+    for (int u = 0; u < SMAX; ++u) {
+        S0 += sv[u][0];
+        S1 += sv[u][1];
+        S2 += sv[u][2];
+    }
+    if (valid && img) {
+        if (lists) {
+            for (int k = w + GSUB * SMAX; k < tot; k += GSUB) {
+                const int jx = k % nX, r = k / nX;
+                const int jy = r % nY, jz = r / nY;
+                const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
+                S0 += p[0];
+                S1 += p[1];
+                S2 += p[2];
             }
         } else {
             const int2 gx = X.gtile[cx], gy = Y.gtile[cy], gz = Z.gtile[cz];
             const int mX = gx.y - gx.x + 1, mY = gy.y - gy.x + 1, mZ = gz.y - gz.x + 1;
-            const int total = (mX > 0 && mY > 0 && mZ > 0) ? mX * mY * mZ : 0;
-            for (int k = sub; k < total; k += 4) {
+            const int mt = (mX > 0 && mY > 0 && mZ > 0) ? mX * mY * mZ : 0;
+            for (int k = w; k < mt; k += GSUB) {
                 const int tx = gx.x + k % mX, ty = gy.x + (k / mX) % mY, tz = gz.x + k / (mX * mY);
                 const int lxo = cx - X.atile0[tx], lyo = cy - Y.atile0[ty], lzo = cz - Z.atile0[tz];
                 const size_t t = (size_t(tz) * Y.nt + ty) * X.nt + tx;
                 const float *p = a.partial + t * a.slot + ((size_t(lzo) * Y.ac + lyo) * X.ac + lxo) * 3;
-                S[0] += p[0];
-                S[1] += p[1];
-                S[2] += p[2];
+                S0 += p[0];
+                S1 += p[1];
+                S2 += p[2];
             }
         }
     }
-    pacc[sub][0][li] = R0;
-    pacc[sub][1][li] = R1;
-    pacc[sub][2][li] = R2;
-    pacc[sub][3][li] = R3;
-    pacc[sub][4][li] = R4;
-    pacc[sub][5][li] = R5;
-    pacc[sub][6][li] = T0;
-    pacc[sub][7][li] = T1;
-    pacc[sub][8][li] = T2;
-    pacc[sub][9][li] = S[0];
-    pacc[sub][10][li] = S[1];
-    pacc[sub][11][li] = S[2];
+    pacc[w][0][lane] = R0;
+    pacc[w][1][lane] = R1;
+    pacc[w][2][lane] = R2;
+    pacc[w][3][lane] = R3;
+    pacc[w][4][lane] = R4;
+    pacc[w][5][lane] = R5;
+    pacc[w][6][lane] = T0;
+    pacc[w][7][lane] = T1;
+    pacc[w][8][lane] = T2;
+    pacc[w][9][lane] = S0;
+    pacc[w][10][lane] = S1;
+    pacc[w][11][lane] = S2;
     __syncthreads();
-    double pval = 0.0;
-    if (sub == 0 && valid) {
-        float v9[12];
+    // warp 0 combines the warps' partials in a fixed order (FP32; the
+    // outputs are widened to double at the store)
+    if (w == 0) {
+        float pval = 0.0f;
+        if (valid) {
+            float v9[GNQ];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) v9[k] = pacc[0][k][li] + pacc[1][k][li] + pacc[2][k][li] + pacc[3][k][li];
-        double gp[3] = {0.0, 0.0, 0.0};
-        if (a.has_penalty) {
-            const float ci0 = float(a.params[i * 3]), ci1 = float(a.params[i * 3 + 1]), ci2 = float(a.params[i * 3 + 2]);
-            float v;
-            if (with_gradient)
-                v = ci0 * v9[0] + ci0 * v9[1] + ci1 * v9[2] + ci1 * v9[3] + ci2 * v9[4] + ci2 * v9[5];
-            else
-                v = ci0 * v9[0] + ci1 * v9[2] + ci2 * v9[4] + ci0 * v9[1] + ci0 * v9[6] + ci1 * v9[3];
-            pval = v;
-            const float g0 = v9[6] + (2.0f * v9[0] + v9[1]);
-            const float g1 = v9[7] + (2.0f * v9[2] + v9[3]);
-            const float g2 = v9[8] + (2.0f * v9[4] + v9[5]);
-            gp[0] = -a.pen_weight * double(g0);
-            gp[1] = -a.pen_weight * double(g1);
-            gp[2] = -a.pen_weight * double(g2);
-        }
-        if (with_gradient) {
+            for (int k = 0; k < GNQ; ++k) {
+                float t = pacc[0][k][lane];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const double gi = image_from_dense ? a.grad_image[i * 3 + k] : a.cost_weight * (-double(v9[9 + k]));
-                a.grad_total[i * 3 + k] = gi + gp[k];
-                if (a.grad_image && !image_from_dense) a.grad_image[i * 3 + k] = gi;
-                if (a.grad_penalty) a.grad_penalty[i * 3 + k] = gp[k];
+                for (int ww = 1; ww < GSUB; ++ww) t += pacc[ww][k][lane];
+                v9[k] = t;
+            }
+            float gp[3] = {0.0f, 0.0f, 0.0f};
+            const float pw = float(a.pen_weight), cw = float(a.cost_weight);
+            if (a.has_penalty) {
+                const float ci0 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].x;
+                const float ci1 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].y;
+                const float ci2 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].z;
+                if (with_gradient)
+                    pval = ci0 * v9[0] + ci0 * v9[1] + ci1 * v9[2] + ci1 * v9[3] + ci2 * v9[4] + ci2 * v9[5];
+                else
+                    pval = ci0 * v9[0] + ci1 * v9[2] + ci2 * v9[4] + ci0 * v9[1] + ci0 * v9[6] + ci1 * v9[3];
+                gp[0] = -pw * (v9[6] + (2.0f * v9[0] + v9[1]));
+                gp[1] = -pw * (v9[7] + (2.0f * v9[2] + v9[3]));
+                gp[2] = -pw * (v9[8] + (2.0f * v9[4] + v9[5]));
+            }
+            if (with_gradient) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double gi = image_from_dense ? a.grad_image[i * 3 + k] : double(cw * -v9[9 + k]);
+                    a.grad_total[i * 3 + k] = gi + double(gp[k]);
+                    if (a.grad_image && !image_from_dense) a.grad_image[i * 3 + k] = gi;
+                    if (a.grad_penalty) a.grad_penalty[i * 3 + k] = double(gp[k]);
+                }
             }
         }
-    }
-    pval = warp_sum(pval);
-    if (lane == 0) red[w] = pval;
-    __syncthreads();
-    if (tid == 0) {
-        a.pen_part[blk] = red[0] + red[1];
-        __threadfence();
-        is_last = (atomicAdd(&a.counters[1], 1u) == unsigned(nblk - 1));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pval += __shfl_xor_sync(FULL, pval, o);
+        if (lane == 0) {
+            a.pen_part[blk] = double(pval);
+            __threadfence();
+            is_last = (atomicAdd(&a.counters[1], 1u) == unsigned(nblk - 1));
+        }
     }
     __syncthreads();
     if (is_last) {
         __threadfence();
-        double sv[1] = {0.0};
-        for (unsigned b = tid; b < unsigned(nblk); b += GT3) sv[0] += ((volatile double *)a.pen_part)[b];
-        block_sum<1>(sv, red);
+        double sv1[1] = {0.0};
+        for (unsigned b = tid; b < unsigned(nblk); b += GT3) sv1[0] += ((volatile double *)a.pen_part)[b];
+        __shared__ double red[GT3 / 32];
+        block_sum<1>(sv1, red);
         if (tid == 0) {
             double *sc = a.scalars;
-            const double pen = a.has_penalty ? sv[0] : 0.0;
+            const double pen = a.has_penalty ? sv1[0] : 0.0;
             sc[SC_PEN] = pen;
             sc[SC_COST_IMG] = a.cost_weight * sc[SC_VALUE];
             sc[SC_COST_PEN] = a.has_penalty ? a.pen_weight * pen : 0.0;
@@ -726,7 +970,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
 #endif
 
 template <int TZ>
-__global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3(EvalArgs a)
+__global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3(const __grid_constant__ EvalArgs a)
 {
     const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     warp3_body<TZ>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, tile);
@@ -787,13 +1031,48 @@ __global__ void __launch_bounds__(GT3) k_gather3_batch(const EvalArgs *__restric
     gather3_body(args[it.x], 1, 0, it.y, nblocks[it.x]);
 }
 
+// float copy of the parameters (the warp and gather kernels read them as
+// float, as the reference's spline evaluation does; FP64 conversions are
+// slow on this GPU, so they are done once per evaluation)
+__global__ void __launch_bounds__(256) k_params_f32(const double *__restrict__ p, float *__restrict__ f, size_t n)
+{
+    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) f[i] = float(p[i]);
+}
+
+// batch: grid (chunks, pairs); pairs whose minimizer has finished are skipped
+__global__ void __launch_bounds__(256) k_params_f32_batch(const EvalArgs *__restrict__ args,
+                                                          const int *__restrict__ active)
+{
+    if (!active[blockIdx.y]) return;
+    const EvalArgs &a = args[blockIdx.y];
+    const size_t n = size_t(a.nc[0]) * a.nc[1] * a.nc[2] * 3;
+    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256)
+        a.params_f[i] = float(a.params[i]);
+}
+
 // ---------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------
+void launch_params_f32_batch(const EvalArgs *args, const int *active, int npairs, size_t max_params, cudaStream_t st)
+{
+    const int chunks = int(std::min<size_t>(64, (max_params + 4095) / 4096));
+    k_params_f32_batch<<<dim3(std::max(chunks, 1), npairs), 256, 0, st>>>(args, active);
+    count_launch();
+}
+
+void launch_params_f32(const EvalArgs &a, cudaStream_t st)
+{
+    const size_t n = size_t(a.nc[0]) * a.nc[1] * a.nc[2] * 3;
+    const int nb = int(std::min<size_t>(1024, (n + 255) / 256));
+    k_params_f32<<<nb, 256, 0, st>>>(a.params, a.params_f, n);
+    count_launch();
+}
 size_t split3_smem(const EvalArgs &a, int which)
 {
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
-    if (which == 0) return size_t(3) * Z.fc * Y.fc * (X.fc + TX3) * sizeof(float);
+    if (which == 0)
+        return size_t(3) * Z.fc * Y.fc * (X.fc + TX3) * sizeof(float) + 128 +
+               size_t(RING_N) * RING_PLANE * sizeof(float);
     return size_t(3) * Z.ac * (TY3 * TX3 + Y.ac * (TX3 + 1)) * sizeof(float);
 }
 
@@ -839,6 +1118,7 @@ void prepare3_z(size_t sm_warp, size_t sm_adj)
 
 void launch_warp3(const EvalArgs &a, cudaStream_t st)
 {
+    launch_params_f32(a, st);
     const size_t sm = split3_smem(a, 0);
     switch (a.ax[2].t) {
     case 4: launch_warp3_z<4>(a, sm, st); break;
@@ -861,7 +1141,7 @@ void launch_adjoint3(const EvalArgs &a, cudaStream_t st)
 
 int gather3_blocks(const EvalArgs &a)
 {
-    return ((a.nc[0] + GB - 1) / GB) * ((a.nc[1] + GB - 1) / GB) * ((a.nc[2] + GB - 1) / GB);
+    return ((a.nc[0] + GBX - 1) / GBX) * ((a.nc[1] + GBY - 1) / GBY) * ((a.nc[2] + GBZ - 1) / GBZ);
 }
 
 void launch_gather3(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st)

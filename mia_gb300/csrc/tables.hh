@@ -17,6 +17,8 @@ struct AxisHost {
     std::vector<int> ftile0;   // nt
     std::vector<int> atile0;   // nt
     std::vector<int> gtile;    // nc x (lo, hi)
+    std::vector<int> glist;    // 3D: nc x GATHER_LMAX partial-slot offset parts
+    std::vector<int> glen;     // 3D: nc list lengths (-1: too long)
 };
 
 int csize_from_rate(int size, float rate);
