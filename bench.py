@@ -538,9 +538,9 @@ def run_gpu(args):
         line["batched"] = {}
         for bname, cpu_s in (("series2d_60", 6.0), ("cohort3d_16", 10.0)):
             bclk = ClockSampler(local)
-            r = measure_batch(bname, 2, 1, local, 0.0 if args.no_cpu_baseline else cpu_s, clocks=bclk)
+            r = measure_batch(bname, 3, 2, local, 0.0 if args.no_cpu_baseline else cpu_s, clocks=bclk)
             r["clocks"] = bclk.summary()
-            r["steps"], r["warmup"] = 2, 1
+            r["steps"], r["warmup"] = 3, 2
             line["batched"][bname] = r
     print(json.dumps(line))
     return 0

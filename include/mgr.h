@@ -75,6 +75,9 @@ const char *mgr_last_error(void);
    cudaStream_t or NULL for a stream owned by the level. */
 mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream,
                             mgr_level **out);
+/* Releases the level.  Its device buffers are freed in stream order: on a
+   caller's stream, work already queued that reads them completes first and
+   destroy does not wait for it; a stream the level created is drained. */
 mgr_status mgr_level_destroy(mgr_level *lvl);
 
 /* Coefficient grid and number of parameters (degrees_of_freedom,

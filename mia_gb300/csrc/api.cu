@@ -125,6 +125,61 @@ static void check_launch(const char *what)
 
 using namespace mgr;
 
+// the divcurl penalty table of the level's grid (3D: translation-invariant
+// cells; 2D: boundary-clipped CSR rows, cached across levels of equal grid)
+static void build_penalty(mgr_level *L)
+{
+    const mgr_level_desc &d = L->d;
+    if (!d.has_penalty) return;
+    const float range[3] = {float(d.size[0]), float(d.size[1]), float(d.dim == 3 ? d.size[2] : 1)};
+    if (d.dim == 3) {
+        std::vector<float> P = build_penalty3(L->nc, range, d.pen_div, d.pen_curl);
+        L->ptable.release();   // kernels queued earlier may still read the old table
+        L->ptable.upload(P, L->stream);
+    } else {
+        const auto t = penalty2_cached(L->nc, range, d.pen_div, d.pen_curl);
+        L->pen_rowptr.release();
+        L->pen_col.release();
+        L->pen_val.release();
+        L->pen_rowptr.upload(t->rowptr, L->stream);
+        L->pen_col.upload(t->col, L->stream);
+        L->pen_val.upload(t->val, L->stream);
+    }
+}
+
+namespace mgr {
+// A new coefficient grid on a level whose images stay (the second pass of a
+// registration level after refine): parameter buffers, tables and penalty
+// are rebuilt, the prefiltered images are kept.  All work is queued on the
+// level's stream.
+void level_set_grid(mgr_level *L, const int csize[3], const int tile[3])
+{
+    const int D = L->d.dim;
+    for (int k = 0; k < D; ++k) {
+        if (csize[k] <= 3) throw std::invalid_argument("coefficient grid must be larger than 3 per axis");
+        L->nc[k] = csize[k];
+        L->d.csize[k] = csize[k];
+    }
+    L->ncoef = size_t(L->nc[0]) * L->nc[1] * L->nc[2];
+    L->nparams = L->ncoef * D;
+    for (int k = 0; k < 3; ++k) L->tile[k] = tile[k];
+    L->params.release();
+    L->params_f.release();
+    L->grad_total.release();
+    L->grad_image.release();
+    L->grad_penalty.release();
+    L->params.alloc(L->nparams, L->stream);
+    if (D == 3) L->params_f.alloc(L->nparams, L->stream);
+    L->grad_total.alloc(L->nparams, L->stream);
+    L->partial.release();
+    L->tile_sums.release();
+    L->pen_part.release();
+    L->build_tables();
+    build_penalty(L);
+    check_launch("level set grid");
+}
+}  // namespace mgr
+
 extern "C" {
 
 const char *mgr_last_error(void) { return g_err.c_str(); }
@@ -197,18 +252,7 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         ck(cudaMemsetAsync(L->counters.p, 0, 8 * sizeof(unsigned), L->stream), "memset");
         ck(cudaMemsetAsync(L->scalars.p, 0, SC_NSLOTS * sizeof(double), L->stream), "memset");
         L->build_tables();
-        if (d.has_penalty) {
-            const float range[3] = {float(d.size[0]), float(d.size[1]), float(d.dim == 3 ? d.size[2] : 1)};
-            if (d.dim == 3) {
-                std::vector<float> P = build_penalty3(L->nc, range, d.pen_div, d.pen_curl);
-                L->ptable.upload(P, L->stream);
-            } else {
-                const auto t = penalty2_cached(L->nc, range, d.pen_div, d.pen_curl);
-                L->pen_rowptr.upload(t->rowptr, L->stream);
-                L->pen_col.upload(t->col, L->stream);
-                L->pen_val.upload(t->val, L->stream);
-            }
-        }
+        build_penalty(L.get());
         check_launch("level create");
     });
     if (st == MGR_OK) *out = L.release();
@@ -219,7 +263,9 @@ mgr_status mgr_level_destroy(mgr_level *lvl)
 {
     if (!lvl) return MGR_OK;
     cudaSetDevice(lvl->device);
-    if (lvl->stream) cudaStreamSynchronize(lvl->stream);
+    // the buffers are freed in stream order, so a caller's stream needs no
+    // synchronisation; a stream the level created is drained before it goes
+    if (lvl->stream && lvl->own_stream) cudaStreamSynchronize(lvl->stream);
     const bool own = lvl->own_stream;
     cudaStream_t s = lvl->stream;
     delete lvl;

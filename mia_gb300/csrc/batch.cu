@@ -19,6 +19,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mgr.h"
@@ -284,6 +285,27 @@ struct PairRun {
     }
 };
 
+// run f(i) for i < n on host threads (the per-pair coefficient resampling
+// is independent host work); the first exception is rethrown
+template <class F>
+void parallel_pairs(size_t n, F f)
+{
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(n, std::thread::hardware_concurrency()));
+    std::vector<std::exception_ptr> err(nt);
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            try {
+                for (size_t i = t; i < n; i += nt) f(i);
+            } catch (...) {
+                err[t] = std::current_exception();
+            }
+        });
+    for (auto &x : th) x.join();
+    for (auto &e : err)
+        if (e) std::rethrow_exception(e);
+}
+
 void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
@@ -511,10 +533,10 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         tr_in.stop();
         for (int shift = levels - 1; shift >= 0; --shift) {
             TraceScope tr_scale("batch: upscale+scale filter", st);
-            for (auto &rp : pairs) {
-                PairRun &r = *rp;
+            parallel_pairs(pairs.size(), [&](size_t i) {
+                PairRun &r = *pairs[i];
                 r.in_pass = false;
-                if (r.identity) continue;
+                if (r.identity) return;
                 for (int k = 0; k < dim; ++k) r.size[k] = r.full.size[k] / (1 << shift);
                 if (shift == levels - 1) {
                     for (int k = 0; k < 3; ++k) r.csize[k] = k < dim ? csize_from_rate(r.size[k], r.full.rate[k]) : 1;
@@ -525,6 +547,10 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                 } else {
                     upscale_params(dim, r.prev, r.size, r.params);
                 }
+            });
+            for (auto &rp : pairs) {
+                PairRun &r = *rp;
+                if (r.identity) continue;
                 const size_t n = size_t(r.size[0]) * r.size[1] * (dim == 3 ? r.size[2] : 1);
                 r.src_l.alloc(n, st);
                 r.ref_l.alloc(n, st);
@@ -534,15 +560,26 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             tr_scale.stop();
             for (int pass = 0; pass < 2; ++pass) {
                 TraceScope tr_lvl("batch: refine+level setup", st);
+                if (pass == 1)
+                    parallel_pairs(pairs.size(), [&](size_t i) {
+                        PairRun &r = *pairs[i];
+                        if (r.identity) return;
+                        int ncn[3] = {1, 1, 1};
+                        for (int k = 0; k < dim; ++k) ncn[k] = refine_csize(r.size[k], r.full.rate[k]);
+                        r.in_pass = refine_params(dim, r.csize, ncn, r.params);
+                        if (r.in_pass)
+                            for (int k = 0; k < 3; ++k) r.csize[k] = ncn[k];
+                    });
                 for (auto &rp : pairs) {
                     PairRun &r = *rp;
                     if (r.identity) continue;
                     if (pass == 1) {
-                        int ncn[3] = {1, 1, 1};
-                        for (int k = 0; k < dim; ++k) ncn[k] = refine_csize(r.size[k], r.full.rate[k]);
-                        r.in_pass = refine_params(dim, r.csize, ncn, r.params);
                         if (!r.in_pass) continue;
-                        for (int k = 0; k < 3; ++k) r.csize[k] = ncn[k];
+                        if (r.lvl) {
+                            // same images as pass 0: only the grid changes
+                            level_set_grid(r.lvl, r.csize, tile);
+                            continue;
+                        }
                     } else {
                         r.in_pass = true;
                     }

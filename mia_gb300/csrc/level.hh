@@ -275,6 +275,8 @@ struct mgr_level {
 namespace mgr {
 // mgr_level_set_images_device without the final stream synchronisation
 void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref);
+// a new coefficient grid (and tile) on a level, images kept
+void level_set_grid(mgr_level *L, const int csize[3], const int tile[3]);
 }  // namespace mgr
 
 namespace mgr {
