@@ -5,10 +5,10 @@
 //
 // All pairs advance in lock step.  One step evaluates the cost+gradient of
 // every unfinished pair at the point its minimizer proposes:
-//   k_min_propose  (one block per pair) the minimizer's next evaluation point
+//   k_min_propose  (blocks x pairs) the minimizer's next evaluation point
 //   warp, adjoint, gather of the split path over a work list of
 //                  (pair, tile) / (pair, block) items covering all pairs
-//   k_min_update   (one block per pair) the minimizer's decision
+//   k_min_update   (blocks x pairs) the minimizer's decision
 // The minimizers (GSL steepest descent as CGSLFDFMinimizer drives it,
 // mia/core/minimizer/gsl.cc:122-156, and CGDSQMinimizer::do_run,
 // mia/core/minimizer/gdsq.cc:60-122) are state machines in device memory, so
@@ -40,6 +40,7 @@ struct MinState {
     double f;       // cost at x
     double step;
     double f_old;   // gdsq
+    double gnorm;   // gsl: |g|, set when g is
     int iter;
     int phase;      // 0: evaluate x0, 1: iterate
     int failed;     // gsl: a trial failed in this iteration
@@ -56,153 +57,212 @@ struct PairVec {
     int n;
 };
 
-__device__ double block_reduce_sum(double v, double *red)
+// The minimizer kernels spread each pair's vectors over blocks of MCH
+// elements (grid: blocks x pairs).  Every block decides from the pair's
+// state as it was at launch; the block that finishes last (per-pair
+// counter) adds the blocks' partial sums in block order and is the only
+// writer of the state, so the decision does not depend on block timing.
+constexpr int MCH = 2048;
+
+struct MinScratch {
+    double *part;     // pairs x nblk x 3: per block sum, sum, max
+    unsigned *count;  // pairs: blocks done
+    int *moved;       // pairs: gsl trial point differs from x
+    int nblk;
+};
+
+// sums of a and b and the maximum of c over the block, returned to every
+// thread (fixed order)
+__device__ void block_reduce3(double &a, double &b, double &c, double *red)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) red[w] = v;
+    a = warp_sum(a);
+    b = warp_sum(b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+    __syncthreads();   // red may still be read by a previous call
+    if (lane == 0) {
+        red[w] = a;
+        red[MT / 32 + w] = b;
+        red[2 * MT / 32 + w] = c;
+    }
     __syncthreads();
-    double s = 0.0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < MT / 32; ++k) s += red[k];
-    __syncthreads();
-    if (threadIdx.x == 0) red[0] = s;
-    __syncthreads();
-    s = red[0];
-    __syncthreads();
-    return s;
+    a = 0.0;
+    b = 0.0;
+    c = 0.0;
+    for (int k = 0; k < MT / 32; ++k) {
+        a += red[k];
+        b += red[MT / 32 + k];
+        c = fmax(c, red[2 * MT / 32 + k]);
+    }
 }
 
-__device__ int block_all(int pred, int *flag)
+// store this block's partials; true in the pair's last block, which then
+// holds the totals (partials added in block order) in a, b, c
+__device__ bool pair_totals(const MinScratch &m, int p, int nb, double &a, double &b, double &c, double *red)
 {
-    if (threadIdx.x == 0) *flag = 1;
+    __shared__ bool last;
+    block_reduce3(a, b, c, red);
+    if (threadIdx.x == 0) {
+        double *pp = m.part + (size_t(p) * m.nblk + blockIdx.x) * 3;
+        pp[0] = a;
+        pp[1] = b;
+        pp[2] = c;
+        __threadfence();
+        last = atomicAdd(&m.count[p], 1u) == unsigned(nb - 1);
+    }
     __syncthreads();
-    if (!pred) *flag = 0;
-    __syncthreads();
-    const int r = *flag;
-    __syncthreads();
-    return r;
+    if (!last) return false;
+    __threadfence();
+    a = 0.0;
+    b = 0.0;
+    c = 0.0;
+    for (int k = threadIdx.x; k < nb; k += MT) {
+        const double *pp = m.part + (size_t(p) * m.nblk + k) * 3;
+        a += __ldcg(pp);
+        b += __ldcg(pp + 1);
+        c = fmax(c, __ldcg(pp + 2));
+    }
+    block_reduce3(a, b, c, red);
+    if (threadIdx.x == 0) m.count[p] = 0;
+    return true;
 }
 
 __global__ void __launch_bounds__(MT) k_min_propose(MinState *st, const PairVec *vec, mgr_minimizer_desc mz,
-                                                    int *active)
+                                                    int *active, MinScratch m)
 {
-    __shared__ double red[MT / 32];
-    __shared__ int flag;
-    const int p = blockIdx.x;
-    MinState &s = st[p];
+    __shared__ double red[3 * MT / 32];
+    const int p = blockIdx.y, tid = threadIdx.x;
     const PairVec v = vec[p];
+    const int nb = (v.n + MCH - 1) / MCH;
+    if (int(blockIdx.x) >= nb) return;
+    const int i0 = blockIdx.x * MCH, i1 = min(v.n, i0 + MCH);
+    const bool lead = blockIdx.x == 0 && tid == 0;
+    const MinState s = st[p];
     if (s.done) {
-        if (threadIdx.x == 0) active[p] = 0;
+        if (lead) active[p] = 0;
         return;
     }
     if (s.phase == 0) {
-        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = v.x[i];
-        if (threadIdx.x == 0) active[p] = 1;
+        for (int i = i0 + tid; i < i1; i += MT) v.xt[i] = v.x[i];
+        if (lead) active[p] = 1;
         return;
     }
     if (mz.kind == MGR_MIN_GSL_SD) {
-        double q = 0.0;
-        for (int i = threadIdx.x; i < v.n; i += MT) q += v.g[i] * v.g[i];
-        const double gnorm = sqrt(block_reduce_sum(q, red));
-        if (gnorm == 0.0 || s.trials >= 2000) {
-            if (threadIdx.x == 0) {
-                s.done = 1;
-                s.status = 1;
+        if (s.gnorm == 0.0 || s.trials >= 2000) {
+            if (lead) {
+                st[p].done = 1;
+                st[p].status = 1;
                 active[p] = 0;
             }
             return;
         }
-        const double a = -s.step / gnorm;
-        int same = 1;
-        for (int i = threadIdx.x; i < v.n; i += MT) {
+        const double a = -s.step / s.gnorm;
+        int mv = 0;
+        for (int i = i0 + tid; i < i1; i += MT) {
             const double x1 = __dadd_rn(v.x[i], __dmul_rn(a, v.g[i]));
             v.xt[i] = x1;
-            if (x1 != v.x[i]) same = 0;
+            if (x1 != v.x[i]) mv = 1;
         }
-        if (block_all(same, &flag)) {
-            if (threadIdx.x == 0) {
-                s.done = 1;
-                s.status = 1;
+        mv = __syncthreads_or(mv);
+        if (tid == 0 && mv) atomicOr(&m.moved[p], 1);
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+        if (!pair_totals(m, p, nb, d0, d1, d2, red)) return;
+        if (tid == 0) {
+            if (atomicExch(&m.moved[p], 0) == 0) {   // the step no longer changes x
+                st[p].done = 1;
+                st[p].status = 1;
                 active[p] = 0;
+            } else {
+                st[p].trials = s.trials + 1;
+                active[p] = 1;
             }
-            return;
-        }
-        if (threadIdx.x == 0) {
-            s.trials += 1;
-            active[p] = 1;
         }
     } else {
         // while (iter++ < maxiter && step > min_step && !success)
         const bool go = (s.iter < mz.maxiter) && (s.step > mz.min_step) && !s.success;
-        __syncthreads();
-        if (threadIdx.x == 0) s.iter += 1;
         if (!go) {
-            if (threadIdx.x == 0) {
-                s.done = 1;
+            if (lead) {
+                st[p].iter = s.iter + 1;
+                st[p].done = 1;
                 active[p] = 0;
             }
             return;
         }
         const double ms = -s.step;
-        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = __dadd_rn(v.xt[i], __dmul_rn(ms, v.g[i]));
-        if (threadIdx.x == 0) active[p] = 1;
+        for (int i = i0 + tid; i < i1; i += MT) v.xt[i] = __dadd_rn(v.xt[i], __dmul_rn(ms, v.g[i]));
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+        if (!pair_totals(m, p, nb, d0, d1, d2, red)) return;
+        if (tid == 0) {
+            st[p].iter = s.iter + 1;
+            active[p] = 1;
+        }
     }
 }
 
 __global__ void __launch_bounds__(MT) k_min_update(MinState *st, const PairVec *vec, mgr_minimizer_desc mz,
-                                                   const int *active)
+                                                   const int *active, MinScratch m)
 {
-    __shared__ double red[MT / 32];
-    __shared__ int flag;
-    const int p = blockIdx.x;
+    __shared__ double red[3 * MT / 32];
+    const int p = blockIdx.y, tid = threadIdx.x;
     if (!active[p]) return;
-    MinState &s = st[p];
     const PairVec v = vec[p];
+    const int nb = (v.n + MCH - 1) / MCH;
+    if (int(blockIdx.x) >= nb) return;
+    const int i0 = blockIdx.x * MCH, i1 = min(v.n, i0 + MCH);
+    const MinState s = st[p];
     const double fe = v.costs[0] + v.costs[1];
+    double q = 0.0, q2 = 0.0, mx = 0.0;
     if (s.phase == 0) {
-        for (int i = threadIdx.x; i < v.n; i += MT) v.g[i] = v.gt[i];
-        int small = 1;
-        if (mz.kind == MGR_MIN_GDSQ)
-            for (int i = threadIdx.x; i < v.n; i += MT)
-                if (fabs(v.gt[i]) >= mz.xtol) small = 0;
-        const int all_small = block_all(small, &flag);
-        if (threadIdx.x == 0) {
-            s.f = fe;
-            s.f_old = fe;
-            s.phase = 1;
-            s.evals += 1;
-            if (mz.kind == MGR_MIN_GDSQ && all_small) s.success |= 1;
+        for (int i = i0 + tid; i < i1; i += MT) {
+            const double gi = v.gt[i];
+            v.g[i] = gi;
+            q += gi * gi;
+            mx = fmax(mx, fabs(gi));
+        }
+        if (!pair_totals(m, p, nb, q, q2, mx, red)) return;
+        if (tid == 0) {
+            MinState &o = st[p];
+            o.f = fe;
+            o.f_old = fe;
+            o.gnorm = sqrt(q);
+            o.phase = 1;
+            o.evals = s.evals + 1;
+            // all |g| < xtol
+            if (mz.kind == MGR_MIN_GDSQ && !(mx >= mz.xtol)) o.success = s.success | 1;
         }
         return;
     }
     if (mz.kind == MGR_MIN_GSL_SD) {
         if (fe > s.f) {
-            if (threadIdx.x == 0) {
-                s.evals += 1;
-                s.failed = 1;
-                s.step *= mz.tol;
+            if (blockIdx.x == 0 && tid == 0) {
+                st[p].evals = s.evals + 1;
+                st[p].failed = 1;
+                st[p].step = s.step * mz.tol;
             }
             return;
         }
-        double q = 0.0;
-        for (int i = threadIdx.x; i < v.n; i += MT) {
+        for (int i = i0 + tid; i < i1; i += MT) {
+            const double gi = v.gt[i];
             v.x[i] = v.xt[i];
-            v.g[i] = v.gt[i];
-            q += v.gt[i] * v.gt[i];
+            v.g[i] = gi;
+            q += gi * gi;
         }
-        const double gn = sqrt(block_reduce_sum(q, red));
-        if (threadIdx.x == 0) {
-            s.evals += 1;
-            s.step *= s.failed ? mz.tol : 2.0;
-            s.f = fe;
-            s.failed = 0;
-            s.trials = 0;
-            s.iter += 1;
-            if (gn < mz.eps) s.done = 1;
-            else if (s.iter >= mz.maxiter) {
-                s.done = 1;
-                s.status = 2;
+        if (!pair_totals(m, p, nb, q, q2, mx, red)) return;
+        if (tid == 0) {
+            MinState &o = st[p];
+            const double gn = sqrt(q);
+            o.gnorm = gn;
+            o.evals = s.evals + 1;
+            o.step = s.step * (s.failed ? mz.tol : 2.0);
+            o.f = fe;
+            o.failed = 0;
+            o.trials = 0;
+            o.iter = s.iter + 1;
+            if (gn < mz.eps) o.done = 1;
+            else if (o.iter >= mz.maxiter) {
+                o.done = 1;
+                o.status = 2;
             }
         }
         return;
@@ -210,52 +270,44 @@ __global__ void __launch_bounds__(MT) k_min_update(MinState *st, const PairVec *
     // gdsq
     if (fe < s.f_old) {
         const double ms = -s.step;
-        double dot = 0.0, nn = 0.0;
-        for (int i = threadIdx.x; i < v.n; i += MT) {
-            const double gs = __dmul_rn(v.g[i], ms);
-            dot += gs * v.gt[i];
-            nn += gs * gs;
-        }
-        const double sum = block_reduce_sum(dot, red);
-        const double nrm = sqrt(block_reduce_sum(nn, red));
-        int gsmall = 1;
-        for (int i = threadIdx.x; i < v.n; i += MT) {
+        for (int i = i0 + tid; i < i1; i += MT) {
+            const double gs = __dmul_rn(v.g[i], ms), gi = v.gt[i];
+            q += gs * gi;
+            q2 += gs * gs;
             v.x[i] = v.xt[i];
-            v.g[i] = v.gt[i];
-            if (fabs(v.gt[i]) >= mz.gtol) gsmall = 0;
+            v.g[i] = gi;
+            mx = fmax(mx, fabs(gi));
         }
-        const int all_gsmall = block_all(gsmall, &flag);
-        double step = s.step;
-        const double aux = s.f_old - fe + sum;
-        if (aux <= 0.0) step *= mz.scale;
-        else step = 0.5 * nrm / aux;
-        int xsmall = 1;
-        const double xt = mz.xtol / step;
-        for (int i = threadIdx.x; i < v.n; i += MT)
-            if (fabs(v.g[i]) >= xt) xsmall = 0;
-        const int all_xsmall = block_all(xsmall, &flag);
-        if (threadIdx.x == 0) {
-            const double frel = s.f_old - fe;
-            s.f_old = fe;
-            s.f = fe;
-            s.step = step;
-            s.evals += 1;
-            if (all_gsmall) s.success |= 2;
-            if (frel < mz.ftolr) s.success |= 4;
-            if (all_xsmall) s.success |= 1;
+        if (!pair_totals(m, p, nb, q, q2, mx, red)) return;
+        if (tid == 0) {
+            MinState &o = st[p];
+            const double nrm = sqrt(q2);
+            double step = s.step;
+            const double aux = s.f_old - fe + q;
+            if (aux <= 0.0) step *= mz.scale;
+            else step = 0.5 * nrm / aux;
+            int success = s.success;
+            if (!(mx >= mz.gtol)) success |= 2;        // all |g| < gtol
+            if (s.f_old - fe < mz.ftolr) success |= 4;
+            if (!(mx >= mz.xtol / step)) success |= 1;  // all |g| < xtol / step
+            o.f_old = fe;
+            o.f = fe;
+            o.step = step;
+            o.evals = s.evals + 1;
+            o.success = success;
         }
     } else {
-        for (int i = threadIdx.x; i < v.n; i += MT) v.xt[i] = v.x[i];
-        const double step = s.step / mz.scale;
-        int xsmall = 1;
-        const double xt = mz.xtol / step;
-        for (int i = threadIdx.x; i < v.n; i += MT)
-            if (fabs(v.g[i]) >= xt) xsmall = 0;
-        const int all_xsmall = block_all(xsmall, &flag);
-        if (threadIdx.x == 0) {
-            s.step = step;
-            s.evals += 1;
-            if (all_xsmall) s.success |= 1;
+        for (int i = i0 + tid; i < i1; i += MT) {
+            v.xt[i] = v.x[i];
+            mx = fmax(mx, fabs(v.g[i]));
+        }
+        if (!pair_totals(m, p, nb, q, q2, mx, red)) return;
+        if (tid == 0) {
+            MinState &o = st[p];
+            const double step = s.step / mz.scale;
+            o.step = step;
+            o.evals = s.evals + 1;
+            if (!(mx >= mz.xtol / step)) o.success = s.success | 1;
         }
     }
 }
@@ -365,7 +417,9 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     DevBuf<PairVec> d_vecs;
     DevBuf<MinState> d_states;
     DevBuf<int2> d_titems, d_gitems;
-    DevBuf<int> d_nblocks, d_active, d_count;
+    DevBuf<int> d_nblocks, d_active, d_count, d_moved;
+    DevBuf<unsigned> d_mcount;
+    DevBuf<double> d_mpart;
     d_args.upload(args, st);
     d_vecs.upload(vecs, st);
     d_states.upload(states, st);
@@ -375,9 +429,20 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     d_active.alloc(np, st);
     d_count.alloc(1, st);
     ck(cudaMemsetAsync(d_active.p, 0, np * sizeof(int), st), "memset");
+    MinScratch msc;
+    msc.nblk = int((max_params + MCH - 1) / MCH);
+    d_mpart.alloc(size_t(np) * msc.nblk * 3, st);
+    d_mcount.alloc(np, st);
+    d_moved.alloc(np, st);
+    ck(cudaMemsetAsync(d_mcount.p, 0, np * sizeof(unsigned), st), "memset");
+    ck(cudaMemsetAsync(d_moved.p, 0, np * sizeof(int), st), "memset");
+    msc.part = d_mpart.p;
+    msc.count = d_mcount.p;
+    msc.moved = d_moved.p;
+    const dim3 mgrid(msc.nblk, np);
 
     auto step = [&]() {
-        k_min_propose<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
+        k_min_propose<<<mgrid, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p, msc);
         if (dim == 3) launch_params_f32_batch(d_args.p, d_active.p, np, max_params, st);
         if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
                                 d_active.p, sm_warp, 0, st))
@@ -385,7 +450,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
                            d_active.p, sm_adj, 1, st);
         launch_gather_batch(dim, d_args.p, d_gitems.p, int(gitems.size()), d_active.p, d_nblocks.p, has_pen, st);
-        k_min_update<<<np, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p);
+        k_min_update<<<mgrid, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p, msc);
         count_launch(2);
     };
     const int chunk = 8;

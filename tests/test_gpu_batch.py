@@ -77,6 +77,24 @@ def test_batch_2d_matches_oracle(kind):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["gsl", "gdsq"])
+def test_batch_minimizer_vectors_span_many_blocks(kind):
+    """fine grids: the minimizer kernels spread each pair's vectors over
+    several blocks of 2048 elements, whose partial sums the pair's last
+    block adds in block order"""
+    from mia_gb300 import registration as R
+    shapes = [(160, 144), (128, 176)]
+    pairs = [_pair2d(61 + 5 * i, s) for i, s in enumerate(shapes)]
+    mg = R.minimizer(kind, maxiter=8, step=0.1)
+    res = R.register_batch(pairs, 2.0, 1, mg, cost="ssd", penalty_weight=10.0)
+    assert min(r[0].size for r in res) > 4 * 2048
+    mo = O.minimizer(kind, maxiter=8, step=0.1)
+    for (mov, ref), (pg, csg, fg, ng) in zip(pairs, res):
+        po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, 2.0, 1, mo, cost="ssd", penalty_weight=10.0)
+        _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
+
+
+@pytest.mark.gpu
 def test_batch_3d_ncc_matches_oracle():
     from mia_gb300 import registration as R
     shapes = [(32, 36, 40), (24, 32, 32), (32, 32, 48)]
