@@ -237,6 +237,24 @@ mgr_status mgr_scale_image(int dim, const int in_size[3], const float *in, const
 mgr_status mgr_normalize_pair(const float *src, const float *ref, size_t n, float *src_out,
                               float *ref_out, double *mean, double *sigma, int *applied, int device);
 
+/* Replaces: C2D/C3DSplineTransformation::refine (mia/3d/transform/spline.cc:
+   360-396, mia/2d/transform/spline.cc:318-353), the coefficient grid growing
+   between the two passes of a registration level: the dim-vector
+   coefficients on the grid nc_old (x fastest, components interleaved,
+   rounded to float) prefiltered and resampled onto nc_new, clamped to the
+   per-component range, stored as float values.  When no axis grows,
+   *grown = 0 and nothing is written; otherwise prod(nc_new) * dim values go
+   to out.  Host arrays; the host restatement the per-pair driver uses. */
+mgr_status mgr_refine_coefficients(int dim, const int nc_old[3], const int nc_new[3], const double *in,
+                                   double *out, int *grown);
+
+/* mgr_refine_coefficients on the device (device pointers, work queued on
+   `stream`, nothing waited for): the same operations, each rounded as
+   written, so the same values.  The batched driver refines its pairs this
+   way. */
+mgr_status mgr_refine_coefficients_device(int dim, const int nc_old[3], const int nc_new[3], const double *d_in,
+                                          double *d_out, int *grown, void *stream);
+
 /* Wait for all work queued on the level's stream. */
 mgr_status mgr_level_sync(mgr_level *lvl);
 

@@ -19,8 +19,12 @@
 namespace mgr {
 
 static std::atomic<unsigned long long> g_launches{0};
-void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
-void count_launch_adjust(unsigned long long value) { g_launches.store(value); }
+static thread_local bool g_capturing = false;
+void count_launch(unsigned n)
+{
+    if (!g_capturing) g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+void count_launch_pause(bool paused) { g_capturing = paused; }
 
 static thread_local std::string g_err;
 void set_last_error(const std::string &msg) { g_err = msg; }

@@ -16,7 +16,12 @@
 // pass as a CUDA graph that is relaunched until every pair has finished.
 // Level transitions (scale filter, upscale, refine) follow
 // TNonrigidRegisterImpl::run (mia/template/nonrigidregister.cxx:193-296).
+#include <array>
+#include <atomic>
+#include <condition_variable>
+#include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -323,9 +328,11 @@ __global__ void k_count_active(const MinState *st, int npairs, int *count)
 struct PairRun {
     mgr_level_desc full{};
     int size[3] = {1, 1, 1}, prev[3] = {0, 0, 0}, csize[3] = {1, 1, 1};
-    DevBuf<float> src, ref, src_n, ref_n, src_l, ref_l;
+    DevBuf<float> src, ref, src_n, ref_n;
     std::vector<double> params;
     mgr_level *lvl = nullptr;
+    std::vector<mgr_level *> made;   // per level (index shift): made ahead, not yet in use
+    bool x_on_device = false;        // x holds the parameters of the next pass (params only sized)
     DevBuf<double> x, g, xt, gt, costs;
     bool identity = false;   // both images of one value
     bool in_pass = false;
@@ -334,6 +341,8 @@ struct PairRun {
     ~PairRun()
     {
         if (lvl) mgr_level_destroy(lvl);
+        for (mgr_level *m : made)
+            if (m) mgr_level_destroy(m);
     }
 };
 
@@ -386,7 +395,9 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     for (int k = 0; k < np; ++k) {
         PairRun &r = *pairs[members[k]];
         const size_t n = r.params.size();
-        r.x.upload(r.params, st);
+        if (r.x_on_device) r.x.alloc(n, st);   // (already there: the refine wrote it)
+        else r.x.upload(r.params, st);
+        r.x_on_device = false;
         r.g.alloc(n, st);
         r.xt.alloc(n, st);
         r.gt.alloc(n, st);
@@ -462,15 +473,21 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     tr_setup.stop();
     if (use_graphs) {
         TraceScope tr("batch: graph capture", st);
-        cudaGraph_t graph;
+        cudaGraph_t graph = nullptr;
         ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture");
-        const unsigned long long before = mgr_kernel_launch_count();
-        for (int i = 0; i < chunk; ++i) step();
-        k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
-        count_launch();
-        ck(cudaStreamEndCapture(st, &graph), "end capture");
         // launches recorded during capture run only when the graph runs
-        count_launch_adjust(before);
+        count_launch_pause(true);
+        try {
+            for (int i = 0; i < chunk; ++i) step();
+        } catch (...) {
+            count_launch_pause(false);
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
+        count_launch_pause(false);
+        ck(cudaStreamEndCapture(st, &graph), "end capture");
         ck(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
         cudaGraphDestroy(graph);
     }
@@ -498,14 +515,31 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     TraceScope tr_back("batch: readback", st);
     if (exec) cudaGraphExecDestroy(exec);
     ck(cudaMemcpyAsync(states.data(), d_states.p, np * sizeof(MinState), cudaMemcpyDeviceToHost, st), "D2H");
+    // every pair's parameters and status flag (counters[6] of its level)
+    // gathered on the device, so that one copy brings them back
+    std::vector<size_t> off(np + 1, 0);
+    for (int k = 0; k < np; ++k) off[k + 1] = off[k] + pairs[members[k]]->params.size();
+    const size_t flags_at = off[np] * sizeof(double);
+    DevBuf<unsigned char> d_back;
+    d_back.alloc(flags_at + size_t(np) * sizeof(unsigned), st);
+    for (int k = 0; k < np; ++k) {
+        PairRun &r = *pairs[members[k]];
+        ck(cudaMemcpyAsync(d_back.p + off[k] * sizeof(double), r.x.p, r.params.size() * sizeof(double),
+                           cudaMemcpyDeviceToDevice, st),
+           "gather");
+        ck(cudaMemcpyAsync(d_back.p + flags_at + size_t(k) * sizeof(unsigned), r.lvl->counters.p + 6,
+                           sizeof(unsigned), cudaMemcpyDeviceToDevice, st),
+           "gather");
+    }
+    std::vector<unsigned char> back(d_back.n);
+    ck(cudaMemcpyAsync(back.data(), d_back.p, back.size(), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "batch sync");
     std::vector<unsigned> flags(np, 0u);
     for (int k = 0; k < np; ++k) {
         PairRun &r = *pairs[members[k]];
-        ck(cudaMemcpyAsync(r.params.data(), r.x.p, r.params.size() * sizeof(double), cudaMemcpyDeviceToHost, st),
-           "D2H");
-        read_status_flag(r.lvl, &flags[k]);
+        std::memcpy(r.params.data(), back.data() + off[k] * sizeof(double), r.params.size() * sizeof(double));
+        std::memcpy(&flags[k], back.data() + flags_at + size_t(k) * sizeof(unsigned), sizeof(unsigned));
     }
-    ck(cudaStreamSynchronize(st), "batch sync");
     for (int k = 0; k < np; ++k) throw_if_flagged(pairs[members[k]]->lvl, flags[k]);
     double vox_evals = 0.0;
     for (int k = 0; k < np; ++k) {
@@ -565,102 +599,305 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             cudaStream_t s;
             ~StreamGuard() { cudaStreamDestroy(s); }
         } guard{st};
+        // the workers that make the levels ahead, each on its own stream (the
+        // streams outlive the pairs: levels not yet moved to st free their
+        // buffers on them)
+        const int nworkers = int(std::max<size_t>(
+            1, std::min<size_t>({size_t(4), size_t(npairs), size_t(std::max(1u, std::thread::hardware_concurrency()))})));
+        struct StreamsGuard {
+            std::vector<cudaStream_t> s;
+            ~StreamsGuard()
+            {
+                for (cudaStream_t x : s) cudaStreamDestroy(x);
+            }
+        } st_prep;
+        for (int w = 0; w < nworkers; ++w) {
+            cudaStream_t x;
+            ck(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "cudaStreamCreate");
+            st_prep.s.push_back(x);
+        }
+        // events.e[w * levels + shift]: worker w made level `shift`;
+        // events.e[nworkers * levels]: the normalised images are on st
+        struct EventGuard {
+            std::vector<cudaEvent_t> e;
+            ~EventGuard()
+            {
+                for (cudaEvent_t x : e) cudaEventDestroy(x);
+            }
+        } events;
+        // events.e[ev_retired + shift]: st is done with the levels retired
+        // when level `shift` starts
+        events.e.assign(size_t(nworkers) * levels + 1 + levels, nullptr);
+        for (auto &e : events.e) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        const size_t ev_normalized = size_t(nworkers) * levels;
+        const size_t ev_retired = ev_normalized + 1;
         int tile[3] = {32, 8, 16};
         if (dim == 2) {
             tile[1] = 16;
             tile[2] = 1;
         }
+        // levels the pairs have left are destroyed on a helper thread while
+        // the next passes run.  Their buffers are freed on a stream other
+        // than st, ordered after their last use by an event on st: st may be
+        // capturing a graph meanwhile, and a capture takes in work that any
+        // thread queues on the stream.
+        struct Reaper {
+            std::vector<mgr_level *> pending;
+            std::thread t;
+            void join()
+            {
+                if (t.joinable()) t.join();
+            }
+            void launch()
+            {
+                join();
+                std::vector<mgr_level *> v;
+                v.swap(pending);
+                if (!v.empty())
+                    t = std::thread([v] {
+                        for (mgr_level *L : v) mgr_level_destroy(L);
+                    });
+            }
+            ~Reaper()
+            {
+                join();
+                for (mgr_level *L : pending) mgr_level_destroy(L);
+            }
+        } reaper;
         std::vector<std::unique_ptr<PairRun>> pairs;
         TraceScope tr_in("batch: input+normalize", st);
+        std::vector<const float *> in_src(npairs), in_ref(npairs);
+        std::vector<float *> out_src(npairs), out_ref(npairs);
+        std::vector<size_t> nvox(npairs);
         for (int p = 0; p < npairs; ++p) {
             std::unique_ptr<PairRun> r(new PairRun);
             r->full = descs[p];
             const size_t n = size_t(descs[p].size[0]) * descs[p].size[1] * (dim == 3 ? descs[p].size[2] : 1);
             r->src_n.alloc(n, st);
             r->ref_n.alloc(n, st);
-            const float *in_src = srcs[p], *in_ref = refs[p];
+            in_src[p] = srcs[p];
+            in_ref[p] = refs[p];
             if (!images_on_device) {
                 r->src.alloc(n, st);
                 r->ref.alloc(n, st);
                 ck(cudaMemcpyAsync(r->src.p, srcs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
                 ck(cudaMemcpyAsync(r->ref.p, refs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
-                in_src = r->src.p;
-                in_ref = r->ref.p;
+                in_src[p] = r->src.p;
+                in_ref[p] = r->ref.p;
             }
-            r->identity = !normalize_pair(in_src, in_ref, n, r->src_n.p, r->ref_n.p, st, nullptr, nullptr);
-            if (r->identity) {
-                for (int k = 0; k < 3; ++k)
-                    r->csize[k] = k < dim ? csize_from_rate(descs[p].size[k], descs[p].rate[k]) : 1;
-                r->params.assign(size_t(r->csize[0]) * r->csize[1] * r->csize[2] * dim, 0.0);
-            }
+            out_src[p] = r->src_n.p;
+            out_ref[p] = r->ref_n.p;
+            nvox[p] = n;
             pairs.push_back(std::move(r));
         }
+        const std::vector<char> varied = normalize_pairs(in_src, in_ref, nvox, out_src, out_ref, st);
+        for (int p = 0; p < npairs; ++p) {
+            PairRun &r = *pairs[p];
+            r.src.release();   // the uploaded images are no longer read (stream-ordered free)
+            r.ref.release();
+            r.identity = !varied[p];
+            if (r.identity) {
+                for (int k = 0; k < 3; ++k)
+                    r.csize[k] = k < dim ? csize_from_rate(descs[p].size[k], descs[p].rate[k]) : 1;
+                r.params.assign(size_t(r.csize[0]) * r.csize[1] * r.csize[2] * dim, 0.0);
+            }
+        }
         tr_in.stop();
+        for (auto &rp : pairs) rp->made.assign(levels, nullptr);
+        // The images and the first level object of every level depend only
+        // on the normalised images, not on the parameters: worker threads
+        // make them (worker w the pairs i = w mod nworkers, on its own
+        // stream), coarsest level first, while the minimizers of the coarser
+        // levels run on st.  A level is ready once every worker has made it:
+        // made[shift] counts them on the host, the workers' events mark it
+        // on the device.
+        ck(cudaEventRecord(events.e[ev_normalized], st), "cudaEventRecord");
+        struct Prep {
+            std::mutex mu;
+            std::condition_variable cv;
+            std::vector<int> made;
+            std::exception_ptr err;
+            std::atomic<bool> stop{false};
+        } prep;
+        prep.made.assign(levels, 0);
+        struct Joiner {   // before the pairs go: the workers end and their device work drains
+            Prep &p;
+            std::vector<cudaStream_t> s;
+            std::vector<std::thread> t;
+            ~Joiner()
+            {
+                p.stop = true;
+                for (auto &x : t)
+                    if (x.joinable()) x.join();
+                for (cudaStream_t x : s) cudaStreamSynchronize(x);
+            }
+        } workers{prep, st_prep.s, {}};
+        auto make_levels = [&](int w) {
+            cudaStream_t sp = st_prep.s[w];
+            try {
+                ck(cudaSetDevice(device), "cudaSetDevice");
+                ck(cudaStreamWaitEvent(sp, events.e[ev_normalized], 0), "cudaStreamWaitEvent");
+                // the grid each level starts with: the coarsest level's from
+                // the rate, then the grid the previous level ended with (its
+                // refine pass grows it or keeps it; upscaling keeps it)
+                std::vector<std::array<int, 3>> grid(pairs.size(), std::array<int, 3>{1, 1, 1});
+                for (int shift = levels - 1; shift >= 0 && !prep.stop; --shift) {
+                    TraceScope tr_make("batch: levels made ahead (workers)", sp);
+                    for (size_t i = size_t(w); i < pairs.size(); i += size_t(nworkers)) {
+                        PairRun &r = *pairs[i];
+                        if (r.identity) continue;
+                        int size[3] = {1, 1, 1}, ncn[3] = {1, 1, 1};
+                        int *csize = grid[i].data();
+                        for (int k = 0; k < dim; ++k) {
+                            size[k] = r.full.size[k] / (1 << shift);
+                            if (shift == levels - 1) {
+                                csize[k] = csize_from_rate(size[k], r.full.rate[k]);
+                                if (csize[k] - 2 <= 1)
+                                    throw std::invalid_argument("coefficient rate too large for the coarsest level");
+                            }
+                            ncn[k] = refine_csize(size[k], r.full.rate[k]);
+                        }
+                        const size_t n = size_t(size[0]) * size[1] * (dim == 3 ? size[2] : 1);
+                        DevBuf<float> src_l, ref_l;   // freed in stream order after the level's copies
+                        src_l.alloc(n, sp);
+                        ref_l.alloc(n, sp);
+                        scale_image(r.src_n.p, r.full.size, src_l.p, size, dim, sp);
+                        scale_image(r.ref_n.p, r.full.size, ref_l.p, size, dim, sp);
+                        mgr_level_desc d = r.full;
+                        for (int k = 0; k < 3; ++k) {
+                            d.size[k] = k < dim ? size[k] : 1;
+                            d.csize[k] = k < dim ? csize[k] : 0;
+                        }
+                        mgr_level *L = nullptr;
+                        ckm(mgr_level_create(&d, device, sp, &L));
+                        r.made[shift] = L;
+                        ckm(mgr_level_set_path(L, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
+                        level_set_images_async(L, src_l.p, ref_l.p);
+                        if (refine_grows(dim, csize, ncn))
+                            for (int k = 0; k < dim; ++k) csize[k] = ncn[k];
+                    }
+                    ck(cudaEventRecord(events.e[size_t(w) * levels + shift], sp), "cudaEventRecord");
+                    tr_make.stop();
+                    std::lock_guard<std::mutex> lk(prep.mu);
+                    prep.made[shift] += 1;
+                    prep.cv.notify_all();
+                }
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(prep.mu);
+                if (!prep.err) prep.err = std::current_exception();
+                prep.cv.notify_all();
+            }
+        };
+        for (int w = 0; w < nworkers; ++w) workers.t.emplace_back(make_levels, w);
         for (int shift = levels - 1; shift >= 0; --shift) {
-            TraceScope tr_scale("batch: upscale+scale filter", st);
-            parallel_pairs(pairs.size(), [&](size_t i) {
-                PairRun &r = *pairs[i];
+            TraceScope tr_scale("batch: upscale", st);
+            for (auto &rp : pairs) {   // (a scaling of the coefficients: cheaper than threads)
+                PairRun &r = *rp;
                 r.in_pass = false;
-                if (r.identity) return;
+                if (r.identity) continue;
                 for (int k = 0; k < dim; ++k) r.size[k] = r.full.size[k] / (1 << shift);
                 if (shift == levels - 1) {
                     for (int k = 0; k < 3; ++k) r.csize[k] = k < dim ? csize_from_rate(r.size[k], r.full.rate[k]) : 1;
-                    for (int k = 0; k < dim; ++k)
-                        if (r.csize[k] - 2 <= 1)
-                            throw std::invalid_argument("coefficient rate too large for the coarsest level");
                     r.params.assign(size_t(r.csize[0]) * r.csize[1] * r.csize[2] * dim, 0.0);
                 } else {
                     upscale_params(dim, r.prev, r.size, r.params);
                 }
-            });
-            for (auto &rp : pairs) {
-                PairRun &r = *rp;
-                if (r.identity) continue;
-                const size_t n = size_t(r.size[0]) * r.size[1] * (dim == 3 ? r.size[2] : 1);
-                r.src_l.alloc(n, st);
-                r.ref_l.alloc(n, st);
-                scale_image(r.src_n.p, r.full.size, r.src_l.p, r.size, dim, st);
-                scale_image(r.ref_n.p, r.full.size, r.ref_l.p, r.size, dim, st);
             }
             tr_scale.stop();
+            {
+                TraceScope tr_wait("batch: wait for the level", st);
+                std::unique_lock<std::mutex> lk(prep.mu);
+                prep.cv.wait(lk, [&] { return prep.err || prep.made[shift] == nworkers; });
+                if (prep.err) std::rethrow_exception(prep.err);
+                lk.unlock();
+                for (int w = 0; w < nworkers; ++w)
+                    ck(cudaStreamWaitEvent(st, events.e[size_t(w) * levels + shift], 0), "cudaStreamWaitEvent");
+            }
             for (int pass = 0; pass < 2; ++pass) {
                 TraceScope tr_lvl("batch: refine+level setup", st);
-                if (pass == 1)
-                    parallel_pairs(pairs.size(), [&](size_t i) {
-                        PairRun &r = *pairs[i];
-                        if (r.identity) return;
+                if (pass == 1) {
+                    // refine: whether a pair's grid grows follows from the
+                    // sizes; the coefficients of the pass-0 result (r.x) are
+                    // refined on the device for all growing pairs at once and
+                    // stay there for the next pass (the host copy is only
+                    // resized: the pass's readback refreshes it).  Grids
+                    // with an axis of fewer than 4 coefficients are refined
+                    // on the host.
+                    std::vector<RefineJobSpec> jobs;
+                    std::vector<PairRun *> on_dev;
+                    std::vector<size_t> at;
+                    size_t total = 0;
+                    for (auto &rp : pairs) {
+                        PairRun &r = *rp;
+                        if (r.identity) continue;
                         int ncn[3] = {1, 1, 1};
                         for (int k = 0; k < dim; ++k) ncn[k] = refine_csize(r.size[k], r.full.rate[k]);
-                        r.in_pass = refine_params(dim, r.csize, ncn, r.params);
-                        if (r.in_pass)
-                            for (int k = 0; k < 3; ++k) r.csize[k] = ncn[k];
-                    });
+                        r.in_pass = refine_grows(dim, r.csize, ncn);
+                        if (!r.in_pass) continue;
+                        bool small = false;
+                        for (int k = 0; k < dim; ++k) small |= r.csize[k] < 4 || ncn[k] < 4;
+                        if (small) {
+                            refine_params(dim, r.csize, ncn, r.params);
+                        } else {
+                            RefineJobSpec j;
+                            for (int k = 0; k < 3; ++k) {
+                                j.nc_old[k] = r.csize[k];
+                                j.nc_new[k] = ncn[k];
+                            }
+                            j.in = r.x.p;
+                            j.out = nullptr;
+                            jobs.push_back(j);
+                            on_dev.push_back(&r);
+                            at.push_back(total);
+                            total += size_t(ncn[0]) * ncn[1] * ncn[2] * dim;
+                        }
+                        for (int k = 0; k < 3; ++k) r.csize[k] = ncn[k];
+                    }
+                    if (!jobs.empty()) {
+                        DevBuf<double> d_new;
+                        d_new.alloc(total, st);
+                        for (size_t j = 0; j < jobs.size(); ++j) jobs[j].out = d_new.p + at[j];
+                        refine_params_device(dim, jobs, st);
+                        for (size_t j = 0; j < jobs.size(); ++j) {
+                            PairRun &r = *on_dev[j];
+                            const size_t n = size_t(r.csize[0]) * r.csize[1] * r.csize[2] * dim;
+                            r.x.alloc(n, st);   // (the old buffer is freed after the refine read it)
+                            ck(cudaMemcpyAsync(r.x.p, d_new.p + at[j], n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                               st),
+                               "refined parameters");
+                            r.params.resize(n);
+                            r.x_on_device = true;
+                        }
+                    }
+                }
+                TraceScope tr_grid(pass == 1 ? "batch: set grid (refine pass)" : "batch: destroy+take level", st);
                 for (auto &rp : pairs) {
                     PairRun &r = *rp;
                     if (r.identity) continue;
                     if (pass == 1) {
-                        if (!r.in_pass) continue;
-                        if (r.lvl) {
-                            // same images as pass 0: only the grid changes
-                            level_set_grid(r.lvl, r.csize, tile);
-                            continue;
-                        }
-                    } else {
-                        r.in_pass = true;
+                        // same images as pass 0: only the grid changes
+                        if (r.in_pass) level_set_grid(r.lvl, r.csize, tile);
+                        continue;
                     }
-                    if (r.lvl) {
-                        mgr_level_destroy(r.lvl);
-                        r.lvl = nullptr;
-                    }
-                    mgr_level_desc d = r.full;
-                    for (int k = 0; k < 3; ++k) {
-                        d.size[k] = k < dim ? r.size[k] : 1;
-                        d.csize[k] = k < dim ? r.csize[k] : 0;
-                    }
-                    ckm(mgr_level_create(&d, device, st, &r.lvl));
-                    ckm(mgr_level_set_path(r.lvl, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
-                    level_set_images_async(r.lvl, r.src_l.p, r.ref_l.p);
+                    r.in_pass = true;
+                    if (r.lvl) reaper.pending.push_back(r.lvl);
+                    r.lvl = r.made[shift];
+                    r.made[shift] = nullptr;
+                    r.lvl->rebind(st);
+                    // the level was made with the grid of this size; the
+                    // parameters carried over from the coarser level keep theirs
+                    if (r.lvl->nc[0] != r.csize[0] || r.lvl->nc[1] != r.csize[1] ||
+                        (dim == 3 && r.lvl->nc[2] != r.csize[2]))
+                        level_set_grid(r.lvl, r.csize, tile);
                 }
+                if (pass == 0 && !reaper.pending.empty()) {
+                    cudaStream_t sr = st_prep.s[0];
+                    ck(cudaEventRecord(events.e[ev_retired + shift], st), "cudaEventRecord");
+                    ck(cudaStreamWaitEvent(sr, events.e[ev_retired + shift], 0), "cudaStreamWaitEvent");
+                    for (mgr_level *L : reaper.pending) L->rebind(sr);
+                    reaper.launch();
+                }
+                tr_grid.stop();
                 tr_lvl.stop();
                 const std::string label = "level " + std::to_string(shift) + " pass " + std::to_string(pass);
                 run_pass(pairs, *mz, dim, tile, use_graphs != 0, st, label.c_str());

@@ -185,23 +185,23 @@ int mirror(int index, int width)
 void filter_line(double *c, int n)
 {
     if (n < 2) return;
-    const double p = std::sqrt(3.0) - 2.0;
-    const double lambda = 2 - p - 1.0 / p;
-    for (int i = 0; i < n; ++i) c[i] *= lambda;
+    const RefineFilterConsts k = refine_filter_consts(n);
+    const double p = k.p;
+    for (int i = 0; i < n; ++i) c[i] *= k.lambda;
     double zn = p;
-    const double iz = 1.0 / p;
-    double z2n = std::pow(p, double(n - 1));
+    const double iz = k.iz;
+    double z2n = k.z2n;
     double sum = c[0] + z2n * c[n - 1];
     z2n *= z2n * iz;
-    for (int k = 1; k < n - 1; ++k) {
-        sum += (zn + z2n) * c[k];
+    for (int k2 = 1; k2 < n - 1; ++k2) {
+        sum += (zn + z2n) * c[k2];
         zn *= p;
         z2n *= iz;
     }
     c[0] = sum / (1.0 - zn * zn);
-    for (int k = 1; k < n; ++k) c[k] += p * c[k - 1];
-    c[n - 1] = (p / (p * p - 1.0)) * (p * c[n - 2] + c[n - 1]);
-    for (int k = n - 2; k >= 0; --k) c[k] = p * (c[k + 1] - c[k]);
+    for (int k2 = 1; k2 < n; ++k2) c[k2] += p * c[k2 - 1];
+    c[n - 1] = k.q * (p * c[n - 2] + c[n - 1]);
+    for (int k2 = n - 2; k2 >= 0; --k2) c[k2] = p * (c[k2 + 1] - c[k2]);
 }
 
 void axis_taps(double x, int width, int idx[4], double w[4])
@@ -221,15 +221,36 @@ void axis_taps(double x, int width, int idx[4], double w[4])
 
 }  // namespace
 
+RefineFilterConsts refine_filter_consts(int n)
+{
+    RefineFilterConsts k;
+    k.p = std::sqrt(3.0) - 2.0;
+    k.lambda = 2 - k.p - 1.0 / k.p;
+    k.iz = 1.0 / k.p;
+    k.q = k.p / (k.p * k.p - 1.0);
+    k.z2n = std::pow(k.p, double(n - 1));
+    return k;
+}
+
+void refine_axis_taps(int n_old, int n_new, std::vector<int> &idx, std::vector<double> &w)
+{
+    const float dx = float(n_old - 1 - 2) / float(n_new - 1 - 2);
+    const float shift = 1.0f;
+    idx.assign(size_t(n_new) * 4, 0);
+    w.assign(size_t(n_new) * 4, 0.0);
+    for (int i = 0; i < n_new; ++i) axis_taps(dx * (float(i) - shift) + shift, n_old, &idx[size_t(i) * 4], &w[size_t(i) * 4]);
+}
+
+bool refine_grows(int dim, const int nc_old[3], const int nc_new[3])
+{
+    for (int k = 0; k < dim; ++k)
+        if (nc_new[k] > nc_old[k]) return true;
+    return false;
+}
+
 bool refine_params(int dim, const int nc_old[3], const int nc_new[3], std::vector<double> &p)
 {
-    bool grows = false;
-    for (int k = 0; k < dim; ++k)
-        if (nc_new[k] > nc_old[k]) grows = true;
-    bool all_le = true;
-    for (int k = 0; k < dim; ++k)
-        if (nc_new[k] > nc_old[k]) all_le = false;
-    if (all_le || !grows) return false;
+    if (!refine_grows(dim, nc_old, nc_new)) return false;
     const int ox = nc_old[0], oy = nc_old[1], oz = dim == 3 ? nc_old[2] : 1;
     const size_t nold = size_t(ox) * oy * oz;
     // coefficients of the vector-valued interpolator: per component, x,
@@ -278,41 +299,85 @@ bool refine_params(int dim, const int nc_old[3], const int nc_new[3], std::vecto
         }
     }
     const int nx = nc_new[0], ny = nc_new[1], nz = dim == 3 ? nc_new[2] : 1;
-    float dxs[3];
-    for (int k = 0; k < dim; ++k) dxs[k] = float(nc_old[k] - 1 - 2) / float(nc_new[k] - 1 - 2);
-    std::vector<double> out(size_t(nx) * ny * nz * dim);
-    const float shift = 1.0f;
-    for (int z = 0; z < nz; ++z)
-        for (int y = 0; y < ny; ++y)
-            for (int x = 0; x < nx; ++x) {
-                const float X[3] = {dxs[0] * (float(x) - shift) + shift, dxs[1] * (float(y) - shift) + shift,
-                                    dim == 3 ? dxs[2] * (float(z) - shift) + shift : 0.0f};
-                int ix[4], iy[4], iz[4] = {0, 0, 0, 0};
-                double wx[4], wy[4], wz[4] = {1, 0, 0, 0};
-                axis_taps(X[0], ox, ix, wx);
-                axis_taps(X[1], oy, iy, wy);
-                if (dim == 3) axis_taps(X[2], oz, iz, wz);
-                double res[3] = {0, 0, 0};
-                const int kz_n = dim == 3 ? 4 : 1;
-                for (int kz = 0; kz < kz_n; ++kz) {
-                    double ry[3] = {0, 0, 0};
-                    for (int ky = 0; ky < 4; ++ky) {
-                        double rx[3] = {0, 0, 0};
-                        for (int kx = 0; kx < 4; ++kx) {
-                            const double *cv = &coef[((size_t(iz[kz]) * oy + iy[ky]) * ox + ix[kx]) * dim];
-                            for (int c = 0; c < dim; ++c) rx[c] += wx[kx] * cv[c];
-                        }
-                        for (int c = 0; c < dim; ++c) ry[c] += wy[ky] * rx[c];
-                    }
-                    for (int c = 0; c < dim; ++c) res[c] += wz[kz] * ry[c];
-                }
-                double *o = &out[((size_t(z) * ny + y) * nx + x) * dim];
-                for (int c = 0; c < dim; ++c) {
-                    double r = res[c];
-                    r = (r >= mn[c]) ? ((r <= mx[c]) ? r : mx[c]) : mn[c];
-                    o[c] = double(float(r));
-                }
+    // taps of every new grid line on each axis (an axis the 2D grid lacks
+    // has the single tap 0 with weight 1)
+    const int nn[3] = {nx, ny, nz}, no[3] = {ox, oy, oz};
+    std::vector<int> ti[3];
+    std::vector<double> tw[3];
+    for (int k = 0; k < 3; ++k) {
+        if (k < dim) {
+            refine_axis_taps(no[k], nn[k], ti[k], tw[k]);
+        } else {
+            ti[k].assign(size_t(nn[k]) * 4, 0);
+            tw[k].assign(size_t(nn[k]) * 4, 0.0);
+            for (int i = 0; i < nn[k]; ++i) tw[k][size_t(i) * 4] = 1.0;
+        }
+    }
+    // The interpolation sums x taps, then y, then z (each sum from 0 in tap
+    // order).  Done as three stages over whole lines, each partial sum is
+    // computed once instead of once per output point, with the same
+    // operands in the same order: the same values.
+    const int kz_n = dim == 3 ? 4 : 1;
+    const size_t rowo = size_t(ox) * dim, rown = size_t(nx) * dim;
+    std::vector<double> r1(size_t(oz) * oy * rown);   // x resampled
+    for (size_t row = 0; row < size_t(oz) * oy; ++row) {
+        const double *src = &coef[row * rowo];
+        double *o = &r1[row * rown];
+        for (int x = 0; x < nx; ++x) {
+            const int *ix = &ti[0][size_t(x) * 4];
+            const double *wx = &tw[0][size_t(x) * 4];
+            for (int c = 0; c < dim; ++c) {
+                double r = 0.0;
+                r += wx[0] * src[size_t(ix[0]) * dim + c];
+                r += wx[1] * src[size_t(ix[1]) * dim + c];
+                r += wx[2] * src[size_t(ix[2]) * dim + c];
+                r += wx[3] * src[size_t(ix[3]) * dim + c];
+                o[size_t(x) * dim + c] = r;
             }
+        }
+    }
+    std::vector<double> r2(size_t(oz) * ny * rown);   // then y
+    for (int z = 0; z < oz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            const int *iy = &ti[1][size_t(y) * 4];
+            const double *wy = &tw[1][size_t(y) * 4];
+            const double *a0 = &r1[(size_t(z) * oy + iy[0]) * rown], *a1 = &r1[(size_t(z) * oy + iy[1]) * rown];
+            const double *a2 = &r1[(size_t(z) * oy + iy[2]) * rown], *a3 = &r1[(size_t(z) * oy + iy[3]) * rown];
+            double *o = &r2[(size_t(z) * ny + y) * rown];
+            for (size_t i = 0; i < rown; ++i) {
+                double r = 0.0;
+                r += wy[0] * a0[i];
+                r += wy[1] * a1[i];
+                r += wy[2] * a2[i];
+                r += wy[3] * a3[i];
+                o[i] = r;
+            }
+        }
+    std::vector<double> out(size_t(nx) * ny * nz * dim);   // then z, clamped, stored as float
+    for (int z = 0; z < nz; ++z) {
+        const int *iz = &ti[2][size_t(z) * 4];
+        const double *wz = &tw[2][size_t(z) * 4];
+        for (int y = 0; y < ny; ++y) {
+            const double *a[4];
+            for (int kz = 0; kz < 4; ++kz) a[kz] = &r2[(size_t(iz[kz]) * ny + y) * rown];
+            double *o = &out[(size_t(z) * ny + y) * rown];
+            for (int x = 0; x < nx; ++x)
+                for (int c = 0; c < dim; ++c) {
+                    const size_t i = size_t(x) * dim + c;
+                    double r = 0.0;
+                    if (kz_n == 4) {
+                        r += wz[0] * a[0][i];
+                        r += wz[1] * a[1][i];
+                        r += wz[2] * a[2][i];
+                        r += wz[3] * a[3][i];
+                    } else {
+                        r += wz[0] * a[0][i];
+                    }
+                    r = (r >= mn[c]) ? ((r <= mx[c]) ? r : mx[c]) : mn[c];
+                    o[i] = double(float(r));
+                }
+        }
+    }
     p.swap(out);
     return true;
 }

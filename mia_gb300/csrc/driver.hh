@@ -45,4 +45,18 @@ void upscale_params(int dim, const int old_size[3], const int new_size[3], std::
 // leaves p unchanged when no axis grows.
 bool refine_params(int dim, const int nc_old[3], const int nc_new[3], std::vector<double> &p);
 
+// whether refine_params moves the coefficients to `nc_new` (some axis grows)
+bool refine_grows(int dim, const int nc_old[3], const int nc_new[3]);
+
+// the constants of refine's line prefilter for a line of n coefficients
+// (pole p = sqrt(3) - 2, gain lambda, 1/p, p / (p^2 - 1), p^(n-1))
+struct RefineFilterConsts {
+    double p, lambda, iz, q, z2n;
+};
+RefineFilterConsts refine_filter_consts(int n);
+
+// refine's resampling taps on one axis: 4 coefficient indices (mirrored at
+// the borders) and cubic B-spline weights per line of the new grid
+void refine_axis_taps(int n_old, int n_new, std::vector<int> &idx, std::vector<double> &w);
+
 }  // namespace mgr

@@ -147,6 +147,7 @@ struct mgr_level {
     DevBuf<unsigned int> counters;
     DevBuf<int> pen_rowptr, pen_col;
     DevBuf<float> grid, force, tmp1, tmp2;   // plain path and standalone force/translate
+    // (rebind() below lists every DevBuf member)
     CUtensorMap tmap{};     // 3D: tensor map of coef_pad
     bool has_tmap = false;
     int slot = 0;
@@ -155,6 +156,25 @@ struct mgr_level {
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_recorded = false;
+    // move the level to stream s: its later work and the stream-ordered
+    // frees of all its buffers go to s (the caller has ordered s after the
+    // work queued on the old stream)
+    void rebind(cudaStream_t s)
+    {
+        if (own_stream) throw std::invalid_argument("a level with its own stream cannot be moved");
+        stream = s;
+        auto re = [s](auto &b) {
+            if (b.p) b.st = s;
+        };
+        re(axis_tables);
+        re(coef), re(coef_pad), re(ref), re(warped), re(minmax), re(partial), re(ptable), re(pen_val), re(params_f);
+        re(mmpart);
+        re(params), re(grad_total), re(grad_image), re(grad_penalty), re(scalars), re(costs), re(tile_sums);
+        re(pen_part), re(means), re(mpart);
+        re(counters);
+        re(pen_rowptr), re(pen_col);
+        re(grid), re(force), re(tmp1), re(tmp2);
+    }
     void record(int k)
     {
         if (timing) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");

@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cuda.h>
+
+#include <vector>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -9,11 +11,11 @@
 
 namespace mgr {
 
-// launch accounting (mgr_kernel_launch_count); count_launch_adjust resets
-// the counter to `value` (launches recorded into a graph are counted when
-// the graph runs)
+// launch accounting (mgr_kernel_launch_count); while a thread records a
+// graph it pauses its own counting (count_launch_pause), and the graph's
+// launches are counted when it runs
 void count_launch(unsigned n = 1);
-void count_launch_adjust(unsigned long long value);
+void count_launch_pause(bool paused);
 
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
 // padded copy with the mirror fold applied in the halo (layout of coef_pad)
@@ -114,5 +116,16 @@ void launch_translate(const EvalArgs &a, const float *force, double *grad, float
                       float *tmp2, cudaStream_t st);                         // plain separable adjoint
 void launch_plain_eval(const EvalArgs &a, float *grid, float *force, float *tmp1, float *tmp2,
                        cudaStream_t st);                                     // PLAIN path image term
+
+// refine_params (driver.cc) on the device for several coefficient fields
+// at once (same operations, each rounded as written: the same values).
+// in: nc_old product x dim parameters, out: nc_new product x dim; device
+// pointers, work queued on st (refine.cu)
+struct RefineJobSpec {
+    int nc_old[3], nc_new[3];
+    const double *in;
+    double *out;
+};
+void refine_params_device(int dim, const std::vector<RefineJobSpec> &jobs, cudaStream_t st);
 
 }  // namespace mgr

@@ -14,45 +14,55 @@
 
 namespace mgr {
 
-// One block of 32 threads owns up to `lb` (<= 32) lines of length n staged
-// in shared memory (pitch n+1); each thread filters one line.  The
-// reference filters each line in a double buffer; FP64 arithmetic runs at a
-// small fraction of the FP32 rate on this GPU, so the recursion runs in
-// float with the same operations: the pole's magnitude (0.268) damps the
-// rounding of every step, and the result differs from the double filter by
-// a few float ulp of the coefficient (the parity tests bound the warped
-// image and costs, which read these coefficients, at 1e-5 / 1e-4).
+// One block of PF_NT threads owns up to `lb` (<= 64) lines of length n,
+// staged in shared memory (odd pitch) by independent coalesced loads: along
+// the line for x lines, across the lines (consecutive x) for y and z lines.
+// One thread per line runs the recursion, then the block stores the lines
+// back the way it loaded them.  The reference filters each line in a double
+// buffer; FP64 arithmetic runs at a small fraction of the FP32 rate on this
+// GPU, so the recursion runs in float with the same operations: the pole's
+// magnitude (0.268) damps the rounding of every step, and the result differs
+// from the double filter by a few float ulp of the coefficient (the parity
+// tests bound the warped image and costs, which read these coefficients, at
+// 1e-5 / 1e-4).
 // axis 0: lines along x (rows, consecutive rows per block);
 // axis 1/2: lines along y/z (columns of consecutive x per block).
-__global__ void __launch_bounds__(32) k_prefilter_lines(float *__restrict__ img, int nx, int ny, int nz,
-                                                        int axis, int lb)
+constexpr int PF_NT = 256;
+
+__global__ void __launch_bounds__(PF_NT) k_prefilter_lines(float *__restrict__ img, int nx, int ny, int nz,
+                                                           int axis, int lb)
 {
     extern __shared__ float sl[];
     const int t = threadIdx.x;
     const size_t nxy = size_t(nx) * ny;
     int n, nl;
-    size_t base, estride;
+    size_t base, lstride, estride;
     if (axis == 0) {
         n = nx;
         const int l0 = blockIdx.x * lb;
         nl = min(lb, ny * nz - l0);
         base = size_t(l0) * nx;
-        for (int l = 0; l < nl; ++l)
-            for (int k = t; k < n; k += 32) sl[l * (n + 1) + k] = img[base + size_t(l) * nx + k];
+        lstride = size_t(nx);
         estride = 1;
     } else {
         const int xb = blockIdx.x * lb;
         const int other = blockIdx.y;
         n = (axis == 1) ? ny : nz;
         base = (axis == 1) ? size_t(other) * nxy + xb : size_t(other) * nx + xb;
+        lstride = 1;
         estride = (axis == 1) ? size_t(nx) : nxy;
         nl = min(lb, nx - xb);
-        if (t < nl)
-            for (int k = 0; k < n; ++k) sl[t * (n + 1) + k] = img[base + t + k * estride];
+    }
+    const int pitch = n | 1;
+    const bool along = axis == 0;
+#pragma unroll 4
+    for (int e = t; e < nl * n; e += PF_NT) {
+        const int l = along ? e / n : e % nl, k = along ? e % n : e / nl;
+        sl[l * pitch + k] = img[base + l * lstride + k * estride];
     }
     __syncthreads();
     if (t < nl && n >= 2) {
-        float *c = sl + t * (n + 1);
+        float *c = sl + t * pitch;
         const float p = float(1.7320508075688772 - 2.0);   // sqrt(3) - 2
         const float lambda = float(2.0 - (1.7320508075688772 - 2.0) - 1.0 / (1.7320508075688772 - 2.0));
         for (int k = 0; k < n; ++k) c[k] *= lambda;
@@ -74,11 +84,9 @@ __global__ void __launch_bounds__(32) k_prefilter_lines(float *__restrict__ img,
         for (int k = n - 2; k >= 0; --k) c[k] = p * (c[k + 1] - c[k]);
     }
     __syncthreads();
-    if (axis == 0) {
-        for (int l = 0; l < nl; ++l)
-            for (int k = t; k < n; k += 32) img[base + size_t(l) * nx + k] = sl[l * (n + 1) + k];
-    } else if (t < nl) {
-        for (int k = 0; k < n; ++k) img[base + t + k * estride] = sl[t * (n + 1) + k];
+    for (int e = t; e < nl * n; e += PF_NT) {
+        const int l = along ? e / n : e % nl, k = along ? e % n : e / nl;
+        img[base + l * lstride + k * estride] = sl[l * pitch + k];
     }
 }
 
@@ -127,10 +135,21 @@ __global__ void __launch_bounds__(256) k_minmax(const float *__restrict__ img, s
     }
 }
 
-static int lines_per_block(int n)
+// lines per block: at most 64 and 64 KB of staged lines, fewer while the
+// launch would have less than two blocks per SM (the recursion of the
+// block's lines is its critical path)
+static int lines_per_block(int n, int lines_total, int blocks_per_line_group)
 {
-    int lb = 32;
-    while (lb > 1 && size_t(lb) * (n + 1) * sizeof(float) > 48 * 1024) lb >>= 1;
+    int lb = 64;
+    while (lb > 1 && size_t(lb) * (n | 1) * sizeof(float) > 64 * 1024) lb >>= 1;
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    while (lb > 8 && size_t((lines_total + lb - 1) / lb) * blocks_per_line_group < size_t(2 * nsm)) lb >>= 1;
     return lb;
 }
 
@@ -143,22 +162,22 @@ void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t 
         attr = true;
     }
     {
-        const int lb = lines_per_block(nx);
         const int nlines = ny * nz;
-        const size_t sm = size_t(lb) * (nx + 1) * sizeof(float);
-        k_prefilter_lines<<<(nlines + lb - 1) / lb, 32, sm, st>>>(img, nx, ny, nz, 0, lb);
+        const int lb = lines_per_block(nx, nlines, 1);
+        const size_t sm = size_t(lb) * (nx | 1) * sizeof(float);
+        k_prefilter_lines<<<(nlines + lb - 1) / lb, PF_NT, sm, st>>>(img, nx, ny, nz, 0, lb);
         count_launch();
     }
     {
-        const int lb = lines_per_block(ny);
-        const size_t sm = size_t(lb) * (ny + 1) * sizeof(float);
-        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, nz), 32, sm, st>>>(img, nx, ny, nz, 1, lb);
+        const int lb = lines_per_block(ny, nx, nz);
+        const size_t sm = size_t(lb) * (ny | 1) * sizeof(float);
+        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, nz), PF_NT, sm, st>>>(img, nx, ny, nz, 1, lb);
         count_launch();
     }
     if (dim == 3 && nz > 1) {
-        const int lb = lines_per_block(nz);
-        const size_t sm = size_t(lb) * (nz + 1) * sizeof(float);
-        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, ny), 32, sm, st>>>(img, nx, ny, nz, 2, lb);
+        const int lb = lines_per_block(nz, nx, ny);
+        const size_t sm = size_t(lb) * (nz | 1) * sizeof(float);
+        k_prefilter_lines<<<dim3((nx + lb - 1) / lb, ny), PF_NT, sm, st>>>(img, nx, ny, nz, 2, lb);
         count_launch();
     }
 }
@@ -182,17 +201,16 @@ __global__ void k_pad_mirror(const float *__restrict__ img, float *__restrict__ 
 
 bool encode_pad_tmap(CUtensorMap *map, const float *pad, int nx, int ny, int nz)
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    // resolved once, thread-safe (levels are made on several host threads)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *f = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        return PFN_cuTensorMapEncodeTiled_v12000(nullptr);
+    }();
     if (!fn) return false;
     const int P = pad_pitch(nx);
     const cuuint64_t dims[3] = {cuuint64_t(P), cuuint64_t(ny + 2 * PAD_H), cuuint64_t(nz + 2 * PAD_H)};

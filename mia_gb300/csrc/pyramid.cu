@@ -53,24 +53,32 @@ __global__ void k_apply_linear(const float *__restrict__ in, float *__restrict__
         out[i] = float(fma(a, double(in[i]), b));
 }
 
-// One warp per block, one line per thread (lb <= 32 lines per block), in
-// float.  The lines are staged in shared memory with an odd pitch; loads and
-// stores are coalesced along x for the x pass (element stride 1) and across
-// the lines otherwise.  Per line: binomial smoothing with half-sample
-// symmetric borders into s, the mirror-boundary cubic prefilter on s in
-// place, then the 4-tap resampling into c (n_out <= n_in).
-__global__ void __launch_bounds__(32) k_scale_lines(const float *__restrict__ in, float *__restrict__ out, int lb,
-                                                    int n_in, int n_out, int nlines, size_t in_line_stride,
-                                                    size_t in_elem_stride, size_t out_line_stride,
-                                                    size_t out_elem_stride, int lines_per_plane,
-                                                    size_t in_plane_stride, size_t out_plane_stride, int gw,
-                                                    const float *gmask, const int4 *idx, const float4 *wts)
+// One block of SCALE_NT threads owns lb consecutive lines (lb <= 64), in
+// float.  Per line: binomial smoothing with half-sample symmetric borders,
+// the mirror-boundary cubic prefilter in place, then the 4-tap resampling
+// (n_out <= n_in).  The block stages its input lines in shared memory with
+// independent coalesced loads (along the line for the x pass, across the
+// lines of consecutive x otherwise), smooths and resamples element-parallel
+// over all its lines, and runs only the prefilter's recursion one thread
+// per line.  Lines sit at an odd pitch (no bank conflicts between lines).
+// The arithmetic of every element is that of a sequential pass over the
+// line.
+constexpr int SCALE_NT = 256;
+
+__global__ void __launch_bounds__(SCALE_NT) k_scale_lines(const float *__restrict__ in, float *__restrict__ out,
+                                                          int lb, int n_in, int n_out, int nlines,
+                                                          size_t in_line_stride, size_t in_elem_stride,
+                                                          size_t out_line_stride, size_t out_elem_stride,
+                                                          int lines_per_plane, size_t in_plane_stride,
+                                                          size_t out_plane_stride, int gw, const float *gmask,
+                                                          const int4 *idx, const float4 *wts)
 {
     extern __shared__ float sl[];
     const int pitch = n_in | 1;
-    const int t = threadIdx.x;
+    const int tid = threadIdx.x;
     const int l0 = blockIdx.x * lb;
     const int nl = min(lb, nlines - l0);
+    const bool along = in_elem_stride == 1;   // x pass: the lines are rows
     auto line_in = [&](int l) {
         const int g = l0 + l, pl = g / lines_per_plane, lp = g % lines_per_plane;
         return in + size_t(pl) * in_plane_stride + size_t(lp) * in_line_stride;
@@ -79,68 +87,62 @@ __global__ void __launch_bounds__(32) k_scale_lines(const float *__restrict__ in
         const int g = l0 + l, pl = g / lines_per_plane, lp = g % lines_per_plane;
         return out + size_t(pl) * out_plane_stride + size_t(lp) * out_line_stride;
     };
+    if (gw < 0) {   // the size does not change on this axis (C1DScalar copies)
+        for (int e = tid; e < nl * n_in; e += SCALE_NT) {
+            const int l = along ? e / n_in : e % nl, k = along ? e % n_in : e / nl;
+            line_out(l)[k * out_elem_stride] = __ldg(line_in(l) + k * in_elem_stride);
+        }
+        return;
+    }
     float *c_all = sl;
     float *s_all = sl + size_t(lb) * pitch;
-    if (in_elem_stride == 1) {
-        for (int l = 0; l < nl; ++l) {
-            const float *src = line_in(l);
-            for (int k = t; k < n_in; k += 32) c_all[l * pitch + k] = src[k];
-        }
-    } else if (t < nl) {
-        const float *src = line_in(t);
-        for (int k = 0; k < n_in; ++k) c_all[t * pitch + k] = src[k * in_elem_stride];
+#pragma unroll 4
+    for (int e = tid; e < nl * n_in; e += SCALE_NT) {
+        const int l = along ? e / n_in : e % nl, k = along ? e % n_in : e / nl;
+        c_all[l * pitch + k] = __ldg(line_in(l) + k * in_elem_stride);
     }
-    __syncwarp();
-    if (t < nl) {
-        float *c = c_all + t * pitch;
-        float *s = s_all + t * pitch;
-        if (gw >= 0) {  // (C1DScalar copies when the size does not change: c is the output)
-            const int m = 2 * gw + 1;
-            for (int i = 0; i < n_in; ++i) {
-                float h = 0.0f;
-                for (int j = 0; j < m; ++j) {
-                    int k = i - gw + j;
-                    if (k < 0) k = -k - 1;
-                    if (k >= n_in) k = 2 * n_in - 1 - k;
-                    h = fmaf(gmask[j], c[k], h);
-                }
-                s[i] = h;
-            }
-            if (n_in >= 2) {
-                const float p = -0.2679491924311227f;            // sqrt(3) - 2
-                const float lambda = 6.0f;                       // 2 - p - 1/p
-                for (int k = 0; k < n_in; ++k) s[k] *= lambda;
-                float zn = p;
-                const float iz = 1.0f / p;
-                float z2n = powf(p, float(n_in - 1));
-                float sum = fmaf(z2n, s[n_in - 1], s[0]);
-                z2n *= z2n * iz;
-                for (int k = 1; k < n_in - 1; ++k) {
-                    sum = fmaf(zn + z2n, s[k], sum);
-                    zn *= p;
-                    z2n *= iz;
-                }
-                s[0] = sum / (1.0f - zn * zn);
-                for (int k = 1; k < n_in; ++k) s[k] = fmaf(p, s[k - 1], s[k]);
-                s[n_in - 1] = (p / (p * p - 1.0f)) * fmaf(p, s[n_in - 2], s[n_in - 1]);
-                for (int k = n_in - 2; k >= 0; --k) s[k] = p * (s[k + 1] - s[k]);
-            }
-            for (int i = 0; i < n_out; ++i) {
-                const int4 ix = idx[i];
-                const float4 w = wts[i];
-                c[i] = fmaf(w.x, s[ix.x], fmaf(w.y, s[ix.y], fmaf(w.z, s[ix.z], w.w * s[ix.w])));
-            }
+    __syncthreads();
+    const int m = 2 * gw + 1;
+    for (int e = tid; e < nl * n_in; e += SCALE_NT) {
+        const int l = along ? e / n_in : e % nl, i = along ? e % n_in : e / nl;
+        const float *c = c_all + l * pitch;
+        float h = 0.0f;
+        for (int j = 0; j < m; ++j) {
+            int k = i - gw + j;
+            if (k < 0) k = -k - 1;
+            if (k >= n_in) k = 2 * n_in - 1 - k;
+            h = fmaf(gmask[j], c[k], h);
         }
+        s_all[l * pitch + i] = h;
     }
-    __syncwarp();
-    if (out_elem_stride == 1) {
-        for (int l = 0; l < nl; ++l) {
-            float *dst = line_out(l);
-            for (int k = t; k < n_out; k += 32) dst[k] = c_all[l * pitch + k];
+    __syncthreads();
+    if (tid < nl && n_in >= 2) {
+        float *s = s_all + tid * pitch;
+        const float p = -0.2679491924311227f;            // sqrt(3) - 2
+        const float lambda = 6.0f;                       // 2 - p - 1/p
+        for (int k = 0; k < n_in; ++k) s[k] *= lambda;
+        float zn = p;
+        const float iz = 1.0f / p;
+        float z2n = powf(p, float(n_in - 1));
+        float sum = fmaf(z2n, s[n_in - 1], s[0]);
+        z2n *= z2n * iz;
+        for (int k = 1; k < n_in - 1; ++k) {
+            sum = fmaf(zn + z2n, s[k], sum);
+            zn *= p;
+            z2n *= iz;
         }
-    } else if (t < nl) {
-        float *dst = line_out(t);
-        for (int k = 0; k < n_out; ++k) dst[k * out_elem_stride] = c_all[t * pitch + k];
+        s[0] = sum / (1.0f - zn * zn);
+        for (int k = 1; k < n_in; ++k) s[k] = fmaf(p, s[k - 1], s[k]);
+        s[n_in - 1] = (p / (p * p - 1.0f)) * fmaf(p, s[n_in - 2], s[n_in - 1]);
+        for (int k = n_in - 2; k >= 0; --k) s[k] = p * (s[k + 1] - s[k]);
+    }
+    __syncthreads();
+    for (int e = tid; e < nl * n_out; e += SCALE_NT) {
+        const int l = along ? e / n_out : e % nl, i = along ? e % n_out : e / nl;
+        const float *s = s_all + l * pitch;
+        const int4 ix = idx[i];
+        const float4 w = wts[i];
+        line_out(l)[i * out_elem_stride] = fmaf(w.x, s[ix.x], fmaf(w.y, s[ix.y], fmaf(w.z, s[ix.z], w.w * s[ix.w])));
     }
 }
 
@@ -167,6 +169,21 @@ int mirror_h(int index, int width)
 void ck(cudaError_t e, const char *what)
 {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// SMs of the current device (cached per device)
+int num_sms()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 1;
+    }
+    return cache[dev];
 }
 
 // per-axis resampling plan of C1DScalar (downscale): gauss half width and
@@ -239,13 +256,17 @@ void scale_axis(const float *in, float *out, const AxisPlan &p, int n_in, int n_
     unsigned char *d = nullptr;
     ck(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
     ck(cudaMemcpyAsync(d, blob.data(), bytes, cudaMemcpyHostToDevice, st), "H2D");
+    // lines per block: at most 64 and 96 KB of staged lines, fewer while
+    // the launch would have less than two blocks per SM (the block's line
+    // recursion is its critical path)
     const int pitch = n_in | 1;
-    int lb = 32;
-    while (lb > 1 && size_t(lb) * 2 * pitch * sizeof(float) > 200 * 1024) lb >>= 1;
+    int lb = 64;
+    while (lb > 1 && size_t(lb) * 2 * pitch * sizeof(float) > 96 * 1024) lb >>= 1;
+    while (lb > 8 && (nlines + lb - 1) / lb < 2 * num_sms()) lb >>= 1;
     const size_t sm = size_t(lb) * 2 * pitch * sizeof(float);
     if (sm > 200 * 1024) throw std::invalid_argument("scale: image line too long");
     cudaFuncSetAttribute(k_scale_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    k_scale_lines<<<(nlines + lb - 1) / lb, 32, sm, st>>>(in, out, lb, n_in, n_out, nlines, ils, ies, ols, oes, lpp,
+    k_scale_lines<<<(nlines + lb - 1) / lb, SCALE_NT, sm, st>>>(in, out, lb, n_in, n_out, nlines, ils, ies, ols, oes, lpp,
                                                          ips, ops, p.gw, reinterpret_cast<const float *>(d),
                                                          reinterpret_cast<const int4 *>(d + o_idx),
                                                          reinterpret_cast<const float4 *>(d + o_wts));
@@ -263,18 +284,16 @@ std::string format_g6(double v)
     return buf;
 }
 
-bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_src_out, float *d_ref_out,
-                    cudaStream_t st, double *mean_out, double *sigma_out)
+namespace {
+
+int pair_sum_blocks(size_t n) { return int(std::min<size_t>(512, (n + 255) / 256)); }
+
+// mean and sigma of the two images together from the per-block partial
+// sums (added in block order); when sigma is not 0 the linear map is
+// queued on both images
+bool normalize_from_sums(const double *part, int nb, const float *d_src, const float *d_ref, size_t n,
+                         float *d_src_out, float *d_ref_out, cudaStream_t st, double *mean_out, double *sigma_out)
 {
-    const int nb = int(std::min<size_t>(512, (n + 255) / 256));
-    double *d_part = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), size_t(nb) * 2 * sizeof(double), st), "cudaMallocAsync");
-    k_pair_sums<<<nb, 256, 0, st>>>(d_src, d_ref, n, d_part);
-    count_launch();
-    std::vector<double> part(size_t(nb) * 2);
-    ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
-    cudaFreeAsync(d_part, st);
-    ck(cudaStreamSynchronize(st), "sync");
     double sum = 0.0, sum2 = 0.0;
     for (int b = 0; b < nb; ++b) {
         sum += part[2 * b];
@@ -296,6 +315,48 @@ bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_s
     count_launch(2);
     ck(cudaGetLastError(), "normalize kernels");
     return true;
+}
+
+}  // namespace
+
+bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_src_out, float *d_ref_out,
+                    cudaStream_t st, double *mean_out, double *sigma_out)
+{
+    const int nb = pair_sum_blocks(n);
+    double *d_part = nullptr;
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), size_t(nb) * 2 * sizeof(double), st), "cudaMallocAsync");
+    k_pair_sums<<<nb, 256, 0, st>>>(d_src, d_ref, n, d_part);
+    count_launch();
+    std::vector<double> part(size_t(nb) * 2);
+    ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    cudaFreeAsync(d_part, st);
+    ck(cudaStreamSynchronize(st), "sync");
+    return normalize_from_sums(part.data(), nb, d_src, d_ref, n, d_src_out, d_ref_out, st, mean_out, sigma_out);
+}
+
+std::vector<char> normalize_pairs(const std::vector<const float *> &src, const std::vector<const float *> &ref,
+                                  const std::vector<size_t> &n, const std::vector<float *> &src_out,
+                                  const std::vector<float *> &ref_out, cudaStream_t st)
+{
+    const size_t np = src.size();
+    std::vector<size_t> off(np + 1, 0);
+    for (size_t i = 0; i < np; ++i) off[i + 1] = off[i] + size_t(pair_sum_blocks(n[i])) * 2;
+    double *d_part = nullptr;
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), std::max<size_t>(off[np], 1) * sizeof(double), st),
+       "cudaMallocAsync");
+    for (size_t i = 0; i < np; ++i) {
+        k_pair_sums<<<pair_sum_blocks(n[i]), 256, 0, st>>>(src[i], ref[i], n[i], d_part + off[i]);
+        count_launch();
+    }
+    std::vector<double> part(off[np]);
+    ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    cudaFreeAsync(d_part, st);
+    ck(cudaStreamSynchronize(st), "sync");
+    std::vector<char> varied(np, 0);
+    for (size_t i = 0; i < np; ++i)
+        varied[i] = normalize_from_sums(part.data() + off[i], pair_sum_blocks(n[i]), src[i], ref[i], n[i], src_out[i],
+                                        ref_out[i], st, nullptr, nullptr);
+    return varied;
 }
 
 void scale_image(const float *d_in, const int in_size[3], float *d_out, const int out_size[3], int dim,

@@ -1,6 +1,8 @@
 // pyramid.hh — multiresolution image preparation (see pyramid.cu).
 #pragma once
 
+#include <vector>
+
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -15,6 +17,14 @@ std::string format_g6(double v);
 // nothing) when both images hold a single value.
 bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_src_out, float *d_ref_out,
                     cudaStream_t st, double *mean_out, double *sigma_out);
+
+// normalize_pair for several pairs with one host synchronisation for all
+// the sums (the same partial sums per pair, so the same results); returns
+// per pair whether its images vary (0: both images of one value, nothing
+// written)
+std::vector<char> normalize_pairs(const std::vector<const float *> &src, const std::vector<const float *> &ref,
+                                  const std::vector<size_t> &n, const std::vector<float *> &src_out,
+                                  const std::vector<float *> &ref_out, cudaStream_t st);
 
 // The `scale` filter (downscaling only); a copy when the sizes agree.
 void scale_image(const float *d_in, const int in_size[3], float *d_out, const int out_size[3], int dim,

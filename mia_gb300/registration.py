@@ -60,6 +60,33 @@ def scale_image(img, out_shape, device=0):
     return out
 
 
+def refine_coefficients(params, nc_old, nc_new):
+    """the spline grid refinement on the host: params (prod(nc_old) * dim,
+    components interleaved, x fastest) onto nc_new; None when no axis grows"""
+    dim = len(nc_old)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    out = np.empty(int(np.prod(nc_new)) * dim)
+    o = (ctypes.c_int * 3)(*(list(nc_old) + [1] * (3 - dim)))
+    n = (ctypes.c_int * 3)(*(list(nc_new) + [1] * (3 - dim)))
+    grown = ctypes.c_int()
+    check(lib().mgr_refine_coefficients(dim, o, n, p.ctypes.data_as(_dp), out.ctypes.data_as(_dp), ctypes.byref(grown)))
+    return out if grown.value else None
+
+
+def refine_coefficients_device(d_params, d_out, nc_old, nc_new, stream=0):
+    """refine_coefficients on device buffers (objects with .data_ptr());
+    queued on `stream` (a CUDA stream handle, 0: the legacy default stream);
+    returns whether the grid grew (d_out written)"""
+    dim = len(nc_old)
+    o = (ctypes.c_int * 3)(*(list(nc_old) + [1] * (3 - dim)))
+    n = (ctypes.c_int * 3)(*(list(nc_new) + [1] * (3 - dim)))
+    grown = ctypes.c_int()
+    check(lib().mgr_refine_coefficients_device(dim, o, n, ctypes.c_void_p(d_params.data_ptr()),
+                                               ctypes.c_void_p(d_out.data_ptr()), ctypes.byref(grown),
+                                               ctypes.c_void_p(stream)))
+    return bool(grown.value)
+
+
 def normalize_pair(src, ref, device=0):
     s = np.ascontiguousarray(src, dtype=np.float32)
     r = np.ascontiguousarray(ref, dtype=np.float32)

@@ -59,6 +59,22 @@ def test_batch_rejects_mixed_dimensions():
 
 
 @pytest.mark.gpu
+def test_batch_rejects_a_rate_too_large_for_the_coarsest_level():
+    """the coarsest level's grid is checked where the levels are made ahead
+    (a worker thread): the error reaches the caller as an argument error"""
+    from mia_gb300 import _lib
+    from mia_gb300 import registration as R
+    pairs = [_pair2d(71, (64, 64)), _pair2d(72, (48, 56))]
+    with pytest.raises(_lib.MgrError) as e:
+        R.register_batch(pairs, 40.0, 3, R.minimizer("gsl", maxiter=2), cost="ssd", penalty_weight=10.0)
+    assert e.value.status == _lib.MGR_ERR_ARG
+    assert "coarsest" in str(e.value)
+    # the library stays usable after the failed call
+    res = R.register_batch(pairs, 16.0, 1, R.minimizer("gsl", maxiter=2), cost="ssd", penalty_weight=10.0)
+    assert len(res) == 2
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["gsl", "gdsq"])
 def test_batch_2d_matches_oracle(kind):
     from mia_gb300 import registration as R

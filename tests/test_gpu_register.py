@@ -31,7 +31,11 @@ def _pair3d(seed, shape=(32, 36, 40), rate=8.0, bias=False):
 
 
 @pytest.mark.parametrize("shape,out", [((80, 96), (40, 48)), ((56, 44), (14, 11)), ((32, 36, 40), (16, 18, 20)),
-                                       ((48, 40, 36), (12, 10, 9))])
+                                       ((48, 40, 36), (12, 10, 9)),
+                                       # many blocks of lines, one axis copied unchanged
+                                       ((40, 150, 200), (40, 75, 100)),
+                                       # odd sizes, factor 4 in x and y, about 2 in z
+                                       ((33, 70, 130), (17, 18, 33))])
 def test_scale_filter_matches_oracle(shape, out):
     from mia_gb300 import registration as R
     from mia_gb300 import synth
