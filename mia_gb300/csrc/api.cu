@@ -158,6 +158,7 @@ namespace mgr {
 // level's stream.
 void level_set_grid(mgr_level *L, const int csize[3], const int tile[3])
 {
+    ck(cudaSetDevice(L->device), "cudaSetDevice");   // (callers may be helper threads)
     const int D = L->d.dim;
     for (int k = 0; k < D; ++k) {
         if (csize[k] <= 3) throw std::invalid_argument("coefficient grid must be larger than 3 per axis");
@@ -182,6 +183,43 @@ void level_set_grid(mgr_level *L, const int csize[3], const int tile[3])
     build_penalty(L);
     check_launch("level set grid");
 }
+mgr_level *level_create_on_images(const mgr_level *S, const int csize[3], cudaStream_t st)
+{
+    ck(cudaSetDevice(S->device), "cudaSetDevice");
+    std::unique_ptr<mgr_level> L(new mgr_level);
+    L->d = S->d;
+    const int D = S->d.dim;
+    for (int k = 0; k < 3; ++k) {
+        L->n[k] = S->n[k];
+        L->nc[k] = k < D ? csize[k] : 1;
+        if (k < D) {
+            if (csize[k] <= 3) throw std::invalid_argument("coefficient grid must be larger than 3 per axis");
+            L->d.csize[k] = csize[k];
+        }
+        L->tile[k] = S->tile[k];
+    }
+    L->N = S->N;
+    L->ncoef = size_t(L->nc[0]) * L->nc[1] * L->nc[2];
+    L->nparams = L->ncoef * D;
+    L->path = S->path;
+    L->device = S->device;
+    L->stream = st;
+    L->images_from = S;
+    L->images_set = true;
+    L->params.alloc(L->nparams, st);
+    if (D == 3) L->params_f.alloc(L->nparams, st);
+    L->grad_total.alloc(L->nparams, st);
+    L->scalars.alloc(SC_NSLOTS, st);
+    L->costs.alloc(2, st);
+    L->counters.alloc(8, st);
+    ck(cudaMemsetAsync(L->counters.p, 0, 8 * sizeof(unsigned), st), "memset");
+    ck(cudaMemsetAsync(L->scalars.p, 0, SC_NSLOTS * sizeof(double), st), "memset");
+    L->build_tables();
+    build_penalty(L.get());
+    check_launch("level create on images");
+    return L.release();
+}
+
 }  // namespace mgr
 
 extern "C" {

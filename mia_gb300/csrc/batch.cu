@@ -331,7 +331,9 @@ struct PairRun {
     DevBuf<float> src, ref, src_n, ref_n;
     std::vector<double> params;
     mgr_level *lvl = nullptr;
+    mgr_level *lvl0 = nullptr;       // the pass-0 level while lvl (refine pass) uses its images
     std::vector<mgr_level *> made;   // per level (index shift): made ahead, not yet in use
+    std::vector<mgr_level *> made1;  // per level: the refine pass's level on made[shift]'s images
     bool x_on_device = false;        // x holds the parameters of the next pass (params only sized)
     DevBuf<double> x, g, xt, gt, costs;
     bool identity = false;   // both images of one value
@@ -341,6 +343,9 @@ struct PairRun {
     ~PairRun()
     {
         if (lvl) mgr_level_destroy(lvl);
+        if (lvl0) mgr_level_destroy(lvl0);
+        for (mgr_level *m : made1)
+            if (m) mgr_level_destroy(m);
         for (mgr_level *m : made)
             if (m) mgr_level_destroy(m);
     }
@@ -424,44 +429,55 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     }
     if (std::max(sm_warp, sm_adj) > 200 * 1024)
         throw std::invalid_argument("coefficient spacing too small for the batched tile shape");
-    DevBuf<EvalArgs> d_args;
-    DevBuf<PairVec> d_vecs;
-    DevBuf<MinState> d_states;
-    DevBuf<int2> d_titems, d_gitems;
-    DevBuf<int> d_nblocks, d_active, d_count, d_moved;
-    DevBuf<unsigned> d_mcount;
-    DevBuf<double> d_mpart;
-    d_args.upload(args, st);
-    d_vecs.upload(vecs, st);
-    d_states.upload(states, st);
-    d_titems.upload(titems, st);
-    d_gitems.upload(gitems, st);
-    d_nblocks.upload(nblocks, st);
-    d_active.alloc(np, st);
-    d_count.alloc(1, st);
-    ck(cudaMemsetAsync(d_active.p, 0, np * sizeof(int), st), "memset");
+    // the pass's tables and counters in one device buffer, filled by one
+    // upload (the counters and flags are zero)
     MinScratch msc;
     msc.nblk = int((max_params + MCH - 1) / MCH);
-    d_mpart.alloc(size_t(np) * msc.nblk * 3, st);
-    d_mcount.alloc(np, st);
-    d_moved.alloc(np, st);
-    ck(cudaMemsetAsync(d_mcount.p, 0, np * sizeof(unsigned), st), "memset");
-    ck(cudaMemsetAsync(d_moved.p, 0, np * sizeof(int), st), "memset");
-    msc.part = d_mpart.p;
-    msc.count = d_mcount.p;
-    msc.moved = d_moved.p;
+    size_t bytes = 0;
+    auto place = [&](size_t sz) {
+        const size_t o = bytes;
+        bytes = (bytes + sz + 255) & ~size_t(255);
+        return o;
+    };
+    const size_t o_args = place(sizeof(EvalArgs) * np), o_vecs = place(sizeof(PairVec) * np);
+    const size_t o_states = place(sizeof(MinState) * np), o_titems = place(sizeof(int2) * titems.size());
+    const size_t o_gitems = place(sizeof(int2) * gitems.size()), o_nblocks = place(sizeof(int) * np);
+    const size_t o_active = place(sizeof(int) * np), o_count = place(sizeof(int));
+    const size_t o_moved = place(sizeof(int) * np), o_mcount = place(sizeof(unsigned) * np);
+    const size_t o_mpart = place(sizeof(double) * size_t(np) * msc.nblk * 3);
+    std::vector<unsigned char> blob(o_mpart, 0);
+    std::memcpy(blob.data() + o_args, args.data(), sizeof(EvalArgs) * np);
+    std::memcpy(blob.data() + o_vecs, vecs.data(), sizeof(PairVec) * np);
+    std::memcpy(blob.data() + o_states, states.data(), sizeof(MinState) * np);
+    std::memcpy(blob.data() + o_titems, titems.data(), sizeof(int2) * titems.size());
+    std::memcpy(blob.data() + o_gitems, gitems.data(), sizeof(int2) * gitems.size());
+    std::memcpy(blob.data() + o_nblocks, nblocks.data(), sizeof(int) * np);
+    DevBuf<unsigned char> d_pass;
+    d_pass.alloc(bytes, st);
+    ck(cudaMemcpyAsync(d_pass.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, st), "pass tables H2D");
+    EvalArgs *d_args = reinterpret_cast<EvalArgs *>(d_pass.p + o_args);
+    PairVec *d_vecs = reinterpret_cast<PairVec *>(d_pass.p + o_vecs);
+    MinState *d_states = reinterpret_cast<MinState *>(d_pass.p + o_states);
+    int2 *d_titems = reinterpret_cast<int2 *>(d_pass.p + o_titems);
+    int2 *d_gitems = reinterpret_cast<int2 *>(d_pass.p + o_gitems);
+    int *d_nblocks = reinterpret_cast<int *>(d_pass.p + o_nblocks);
+    int *d_active = reinterpret_cast<int *>(d_pass.p + o_active);
+    int *d_count = reinterpret_cast<int *>(d_pass.p + o_count);
+    msc.part = reinterpret_cast<double *>(d_pass.p + o_mpart);
+    msc.count = reinterpret_cast<unsigned *>(d_pass.p + o_mcount);
+    msc.moved = reinterpret_cast<int *>(d_pass.p + o_moved);
     const dim3 mgrid(msc.nblk, np);
 
     auto step = [&]() {
-        k_min_propose<<<mgrid, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p, msc);
-        if (dim == 3) launch_params_f32_batch(d_args.p, d_active.p, np, max_params, st);
-        if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
-                                d_active.p, sm_warp, 0, st))
+        k_min_propose<<<mgrid, MT, 0, st>>>(d_states, d_vecs, mz, d_active, msc);
+        if (dim == 3) launch_params_f32_batch(d_args, d_active, np, max_params, st);
+        if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
+                                d_active, sm_warp, 0, st))
             throw std::invalid_argument("tile shape not compiled in");
-        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args.p, d_titems.p, int(titems.size()),
-                           d_active.p, sm_adj, 1, st);
-        launch_gather_batch(dim, d_args.p, d_gitems.p, int(gitems.size()), d_active.p, d_nblocks.p, has_pen, st);
-        k_min_update<<<mgrid, MT, 0, st>>>(d_states.p, d_vecs.p, mz, d_active.p, msc);
+        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
+                           d_active, sm_adj, 1, st);
+        launch_gather_batch(dim, d_args, d_gitems, int(gitems.size()), d_active, d_nblocks, has_pen, st);
+        k_min_update<<<mgrid, MT, 0, st>>>(d_states, d_vecs, mz, d_active, msc);
         count_launch(2);
     };
     const int chunk = 8;
@@ -485,7 +501,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
             if (graph) cudaGraphDestroy(graph);
             throw;
         }
-        k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
+        k_count_active<<<1, 32, 0, st>>>(d_states, np, d_count);
         count_launch_pause(false);
         ck(cudaStreamEndCapture(st, &graph), "end capture");
         ck(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
@@ -499,12 +515,12 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
             count_launch(kernels_per_chunk);
         } else {
             for (int i = 0; i < chunk; ++i) step();
-            k_count_active<<<1, 32, 0, st>>>(d_states.p, np, d_count.p);
+            k_count_active<<<1, 32, 0, st>>>(d_states, np, d_count);
             count_launch();
         }
         steps += chunk;
         int active = 0;
-        ck(cudaMemcpyAsync(&active, d_count.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaMemcpyAsync(&active, d_count, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
         ck(cudaStreamSynchronize(st), "batch sync");
         if (active == 0) break;
     }
@@ -514,7 +530,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_steps0).count();
     TraceScope tr_back("batch: readback", st);
     if (exec) cudaGraphExecDestroy(exec);
-    ck(cudaMemcpyAsync(states.data(), d_states.p, np * sizeof(MinState), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaMemcpyAsync(states.data(), d_states, np * sizeof(MinState), cudaMemcpyDeviceToHost, st), "D2H");
     // every pair's parameters and status flag (counters[6] of its level)
     // gathered on the device, so that one copy brings them back
     std::vector<size_t> off(np + 1, 0);
@@ -703,7 +719,10 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             }
         }
         tr_in.stop();
-        for (auto &rp : pairs) rp->made.assign(levels, nullptr);
+        for (auto &rp : pairs) {
+            rp->made.assign(levels, nullptr);
+            rp->made1.assign(levels, nullptr);
+        }
         // The images and the first level object of every level depend only
         // on the normalised images, not on the parameters: worker threads
         // make them (worker w the pairs i = w mod nworkers, on its own
@@ -773,8 +792,11 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                         r.made[shift] = L;
                         ckm(mgr_level_set_path(L, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
                         level_set_images_async(L, src_l.p, ref_l.p);
-                        if (refine_grows(dim, csize, ncn))
+                        if (refine_grows(dim, csize, ncn)) {
+                            // the refine pass's grid, on the same images
+                            r.made1[shift] = level_create_on_images(L, ncn, sp);
                             for (int k = 0; k < dim; ++k) csize[k] = ncn[k];
+                        }
                     }
                     ck(cudaEventRecord(events.e[size_t(w) * levels + shift], sp), "cudaEventRecord");
                     tr_make.stop();
@@ -875,12 +897,26 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                     PairRun &r = *rp;
                     if (r.identity) continue;
                     if (pass == 1) {
-                        // same images as pass 0: only the grid changes
-                        if (r.in_pass) level_set_grid(r.lvl, r.csize, tile);
+                        // same images as pass 0, the refined grid: the level
+                        // made ahead on pass 0's images, else a new grid on
+                        // the pass-0 level
+                        if (!r.in_pass) continue;
+                        mgr_level *L1 = r.made1[shift];
+                        if (L1 && L1->nc[0] == r.csize[0] && L1->nc[1] == r.csize[1] &&
+                            (dim == 2 || L1->nc[2] == r.csize[2])) {
+                            r.made1[shift] = nullptr;
+                            r.lvl0 = r.lvl;
+                            r.lvl = L1;
+                            L1->rebind(st);
+                        } else {
+                            level_set_grid(r.lvl, r.csize, tile);
+                        }
                         continue;
                     }
                     r.in_pass = true;
                     if (r.lvl) reaper.pending.push_back(r.lvl);
+                    if (r.lvl0) reaper.pending.push_back(r.lvl0);
+                    r.lvl0 = nullptr;
                     r.lvl = r.made[shift];
                     r.made[shift] = nullptr;
                     r.lvl->rebind(st);

@@ -185,29 +185,35 @@ struct mgr_level {
             if (e) cudaEventDestroy(e);
     }
 
+    // a level made on another level's images (the refine pass of a batched
+    // registration level): the image buffers are that level's, which
+    // outlives this one; only one of the two is evaluated at a time
+    const mgr_level *images_from = nullptr;
+
     EvalArgs args() const
     {
+        const mgr_level &I = images_from ? *images_from : *this;
         EvalArgs a{};
-        a.tmap = tmap;
-        a.has_tmap = has_tmap;
+        a.tmap = I.tmap;
+        a.has_tmap = I.has_tmap;
         a.dim = d.dim;
         for (int k = 0; k < 3; ++k) {
             a.n[k] = n[k];
             a.nc[k] = nc[k];
             a.ax[k] = ax[k].view();
         }
-        a.coef_img = coef.p;
-        a.coef_pad = coef_pad.p;
+        a.coef_img = I.coef.p;
+        a.coef_pad = I.coef_pad.p;
         a.pad_rows = n[1] + 2 * PAD_H;
-        a.ref = ref.p;
-        a.warped = warped.p;
-        a.minmax = minmax.p;
+        a.ref = I.ref.p;
+        a.warped = I.warped.p;
+        a.minmax = I.minmax.p;
         a.params = params.p;
         a.params_f = params_f.p;
         a.cost = d.cost;
         a.ssd_norm = d.ssd_norm;
         a.cost_weight = d.cost_weight;
-        a.centers = means.p;
+        a.centers = I.means.p;
         a.partial = partial.p;
         a.slot = slot;
         a.tile_sums = tile_sums.p;
@@ -297,6 +303,9 @@ namespace mgr {
 void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref);
 // a new coefficient grid (and tile) on a level, images kept
 void level_set_grid(mgr_level *L, const int csize[3], const int tile[3]);
+// a level with the coefficient grid csize on the images of level S (same
+// sizes, cost, penalty, path and tile; S must outlive it), made on stream st
+mgr_level *level_create_on_images(const mgr_level *S, const int csize[3], cudaStream_t st);
 }  // namespace mgr
 
 namespace mgr {

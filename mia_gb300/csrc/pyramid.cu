@@ -31,20 +31,57 @@ struct Wt4 {
     double x, y, z, w;
 };
 
-__global__ void k_pair_sums(const float *__restrict__ a, const float *__restrict__ b, size_t n, double *part)
+// per-block sums of a + b and a^2 + b^2 in double: block `blk` of `nblk`
+// takes elements blk * 256 + t + k * nblk * 256
+__device__ __forceinline__ void pair_sums_body(const float *__restrict__ a, const float *__restrict__ b, size_t n,
+                                               double *part, int blk, int nblk)
 {
     __shared__ double red[2 * 8];
     double v[2] = {0.0, 0.0};
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    for (size_t i = blk * size_t(256) + threadIdx.x; i < n; i += size_t(nblk) * 256) {
         const double fa = a[i], fb = b[i];
         v[0] += fa + fb;
         v[1] += fa * fa + fb * fb;
     }
     block_sum<2>(v, red);
     if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = v[0];
-        part[2 * blockIdx.x + 1] = v[1];
+        part[2 * blk] = v[0];
+        part[2 * blk + 1] = v[1];
     }
+}
+
+__global__ void __launch_bounds__(256) k_pair_sums(const float *__restrict__ a, const float *__restrict__ b, size_t n,
+                                                   double *part)
+{
+    pair_sums_body(a, b, n, part, blockIdx.x, gridDim.x);
+}
+
+// the normalisation of several pairs: per pair its images, block count of
+// the sums, partial-sum slots and the linear map out = a * in + b
+struct NormJob {
+    const float *src, *ref;
+    float *src_out, *ref_out;
+    size_t n;
+    double *part;
+    int nb, varied;
+    double a, b;
+};
+
+__global__ void __launch_bounds__(256) k_pair_sums_batch(const NormJob *jobs)
+{
+    const NormJob &J = jobs[blockIdx.y];
+    if (int(blockIdx.x) >= J.nb) return;
+    pair_sums_body(J.src, J.ref, J.n, J.part, blockIdx.x, J.nb);
+}
+
+__global__ void __launch_bounds__(256) k_apply_linear_batch(const NormJob *jobs)
+{
+    const NormJob &J = jobs[blockIdx.y];
+    if (!J.varied) return;
+    const float *in = blockIdx.z ? J.ref : J.src;
+    float *out = blockIdx.z ? J.ref_out : J.src_out;
+    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < J.n; i += size_t(gridDim.x) * 256)
+        out[i] = float(fma(J.a, double(in[i]), J.b));
 }
 
 __global__ void k_apply_linear(const float *__restrict__ in, float *__restrict__ out, size_t n, double a, double b)
@@ -289,15 +326,14 @@ namespace {
 int pair_sum_blocks(size_t n) { return int(std::min<size_t>(512, (n + 255) / 256)); }
 
 // mean and sigma of the two images together from the per-block partial
-// sums (added in block order); when sigma is not 0 the linear map is
-// queued on both images
-bool normalize_from_sums(const double *part, int nb, const float *d_src, const float *d_ref, size_t n,
-                         float *d_src_out, float *d_ref_out, cudaStream_t st, double *mean_out, double *sigma_out)
+// sums (added in block order) and the linear map a * x + b; false when
+// sigma is 0
+bool norm_map(const double *part, int nb, size_t n, double &a, double &b, double *mean_out, double *sigma_out)
 {
     double sum = 0.0, sum2 = 0.0;
-    for (int b = 0; b < nb; ++b) {
-        sum += part[2 * b];
-        sum2 += part[2 * b + 1];
+    for (int k = 0; k < nb; ++k) {
+        sum += part[2 * k];
+        sum2 += part[2 * k + 1];
     }
     const double nn = 2.0 * double(n);
     const double mean = sum / nn;
@@ -307,8 +343,16 @@ bool normalize_from_sums(const double *part, int nb, const float *d_src, const f
     if (sigma == 0.0) return false;
     // the reference passes a and b through "convert:...,b=<v>,a=<v>" with
     // the default stream precision (6 significant digits)
-    const double b = std::stod(format_g6(-mean / sigma));
-    const double a = std::stod(format_g6(1.0 / sigma));
+    b = std::stod(format_g6(-mean / sigma));
+    a = std::stod(format_g6(1.0 / sigma));
+    return true;
+}
+
+bool normalize_from_sums(const double *part, int nb, const float *d_src, const float *d_ref, size_t n,
+                         float *d_src_out, float *d_ref_out, cudaStream_t st, double *mean_out, double *sigma_out)
+{
+    double a = 0.0, b = 0.0;
+    if (!norm_map(part, nb, n, a, b, mean_out, sigma_out)) return false;
     const int nb2 = int(std::min<size_t>(4096, (n + 255) / 256));
     k_apply_linear<<<nb2, 256, 0, st>>>(d_src, d_src_out, n, a, b);
     k_apply_linear<<<nb2, 256, 0, st>>>(d_ref, d_ref_out, n, a, b);
@@ -339,23 +383,59 @@ std::vector<char> normalize_pairs(const std::vector<const float *> &src, const s
                                   const std::vector<float *> &ref_out, cudaStream_t st)
 {
     const size_t np = src.size();
-    std::vector<size_t> off(np + 1, 0);
-    for (size_t i = 0; i < np; ++i) off[i + 1] = off[i] + size_t(pair_sum_blocks(n[i])) * 2;
-    double *d_part = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), std::max<size_t>(off[np], 1) * sizeof(double), st),
-       "cudaMallocAsync");
-    for (size_t i = 0; i < np; ++i) {
-        k_pair_sums<<<pair_sum_blocks(n[i]), 256, 0, st>>>(src[i], ref[i], n[i], d_part + off[i]);
-        count_launch();
-    }
-    std::vector<double> part(off[np]);
-    ck(cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
-    cudaFreeAsync(d_part, st);
-    ck(cudaStreamSynchronize(st), "sync");
     std::vector<char> varied(np, 0);
-    for (size_t i = 0; i < np; ++i)
-        varied[i] = normalize_from_sums(part.data() + off[i], pair_sum_blocks(n[i]), src[i], ref[i], n[i], src_out[i],
-                                        ref_out[i], st, nullptr, nullptr);
+    if (np == 0) return varied;
+    // one launch of the sums for all pairs (each pair with the block count
+    // of its own launch, so the same partial sums), one copy back, one
+    // launch of the linear maps
+    std::vector<NormJob> jobs(np);
+    size_t nparts = 0, maxnb = 1, maxn = 1;
+    for (size_t i = 0; i < np; ++i) {
+        NormJob &J = jobs[i];
+        J.src = src[i];
+        J.ref = ref[i];
+        J.src_out = src_out[i];
+        J.ref_out = ref_out[i];
+        J.n = n[i];
+        J.nb = pair_sum_blocks(n[i]);
+        J.varied = 0;
+        J.a = J.b = 0.0;
+        nparts += size_t(J.nb) * 2;
+        maxnb = std::max<size_t>(maxnb, J.nb);
+        maxn = std::max<size_t>(maxn, n[i]);
+    }
+    const size_t o_part = ((sizeof(NormJob) * np + 255) / 256) * 256;
+    unsigned char *d = nullptr;
+    ck(cudaMallocAsync(reinterpret_cast<void **>(&d), o_part + nparts * sizeof(double), st), "cudaMallocAsync");
+    double *d_part = reinterpret_cast<double *>(d + o_part);
+    size_t off = 0;
+    std::vector<size_t> at(np);
+    for (size_t i = 0; i < np; ++i) {
+        at[i] = off;
+        jobs[i].part = d_part + off;
+        off += size_t(jobs[i].nb) * 2;
+    }
+    ck(cudaMemcpyAsync(d, jobs.data(), sizeof(NormJob) * np, cudaMemcpyHostToDevice, st), "H2D");
+    k_pair_sums_batch<<<dim3(unsigned(maxnb), unsigned(np)), 256, 0, st>>>(reinterpret_cast<const NormJob *>(d));
+    count_launch();
+    std::vector<double> part(nparts);
+    ck(cudaMemcpyAsync(part.data(), d_part, nparts * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "sync");
+    bool any = false;
+    for (size_t i = 0; i < np; ++i) {
+        NormJob &J = jobs[i];
+        J.varied = norm_map(part.data() + at[i], J.nb, J.n, J.a, J.b, nullptr, nullptr) ? 1 : 0;
+        varied[i] = char(J.varied);
+        any |= J.varied != 0;
+    }
+    if (any) {
+        ck(cudaMemcpyAsync(d, jobs.data(), sizeof(NormJob) * np, cudaMemcpyHostToDevice, st), "H2D");
+        const unsigned nb2 = unsigned(std::min<size_t>(4096, (maxn + 255) / 256));
+        k_apply_linear_batch<<<dim3(nb2, unsigned(np), 2), 256, 0, st>>>(reinterpret_cast<const NormJob *>(d));
+        count_launch();
+        ck(cudaGetLastError(), "normalize kernels");
+    }
+    cudaFreeAsync(d, st);
     return varied;
 }
 
