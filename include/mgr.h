@@ -132,6 +132,12 @@ mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad)
    reference: it chooses between implementations of the same result. */
 mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z);
 
+/* The tile shape the level's split path uses: the autotuner's choice for
+   the nearest tuned case (mia_gb300/tiles.json) when it fits the level's
+   coefficient spacing, else the shared-memory fit rule; or the shape last
+   given to mgr_level_set_path. */
+mgr_status mgr_level_tile(const mgr_level *lvl, int tile[3]);
+
 /* Kernel timing for profiling: with `enable` set, every evaluation records
    CUDA events around its kernels on the level's stream.
    mgr_level_kernel_times waits for the last evaluation and writes the

@@ -16,8 +16,10 @@ OUT = os.path.join(HERE, "libmgr.so")
 BUILD = os.path.join(HERE, "_build")
 
 CU_SOURCES = ["api.cu", "eval.cu", "split.cu", "split3.cu", "gather.cu", "prefilter.cu", "noalloc.cu", "pyramid.cu", "register.cu", "batch.cu", "refine.cu"]
-CXX_SOURCES = ["tables.cc", "driver.cc"]
+CXX_SOURCES = ["tables.cc", "driver.cc", "tune.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+TILES_JSON = os.path.join(HERE, "tiles.json")
+TILE_TABLE = os.path.join(BUILD, "tile_table.inc")
 
 
 def nvcc():
@@ -39,6 +41,23 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def write_tile_table():
+    """tiles.json (the autotuner's committed choices) as C initialisers for
+    tune.cc; an empty table when the file is absent"""
+    import json
+    lines = ["// generated from tiles.json by build.py"]
+    if os.path.exists(TILES_JSON):
+        with open(TILES_JSON) as f:
+            doc = json.load(f)
+        for e in doc.get("entries", []):
+            t = list(e["tile"]) + [1] * (3 - len(e["tile"]))
+            lines.append("{%d, %.9g, %.9g, {%d, %d, %d}}," % (e["dim"], e["spacing"], e["voxels"], t[0], t[1], t[2]))
+    text = "\n".join(lines) + "\n"
+    if not os.path.exists(TILE_TABLE) or open(TILE_TABLE).read() != text:
+        with open(TILE_TABLE, "w") as f:
+            f.write(text)
+
+
 def build(force=False, verbose=False, extra_nvcc=()):
     os.makedirs(BUILD, exist_ok=True)
     # objects built on another host architecture are never reused
@@ -49,6 +68,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         force = True
     with open(stamp, "w") as f:
         f.write(arch)
+    write_tile_table()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hh", ".cuh", ".h"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "mgr.h"))
     jobs, objs = [], []
@@ -63,8 +83,9 @@ def build(force=False, verbose=False, extra_nvcc=()):
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
-        if force or _stale(o, [s] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c", s, "-o", o])
+        if force or _stale(o, [s, TILE_TABLE] + headers):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", BUILD, "-c", s, "-o",
+                         o])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out:

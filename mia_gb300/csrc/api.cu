@@ -260,13 +260,7 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         L->N = size_t(L->n[0]) * L->n[1] * L->n[2];
         L->ncoef = size_t(L->nc[0]) * L->nc[1] * L->nc[2];
         L->nparams = L->ncoef * d.dim;
-        if (d.dim == 2) {
-            L->tile[0] = 32;
-            L->tile[1] = 16;
-            L->tile[2] = 1;
-        } else {
-            L->choose_tile3();
-        }
+        L->choose_tile();
         L->device = device;
         ck(cudaSetDevice(device), "cudaSetDevice");
         configure_pool(device);
@@ -600,6 +594,13 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
             ck(cudaStreamSynchronize(lvl->stream), "sync");
         }
     });
+}
+
+mgr_status mgr_level_tile(const mgr_level *lvl, int tile[3])
+{
+    if (!lvl || !tile) return fail(MGR_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k) tile[k] = lvl->tile[k];
+    return MGR_OK;
 }
 
 mgr_status mgr_level_set_timing(mgr_level *lvl, int enable)

@@ -647,11 +647,15 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         for (auto &e : events.e) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         const size_t ev_normalized = size_t(nworkers) * levels;
         const size_t ev_retired = ev_normalized + 1;
-        int tile[3] = {32, 8, 16};
-        if (dim == 2) {
-            tile[1] = 16;
-            tile[2] = 1;
-        }
+        // one tile for all pairs and levels (the batch kernels take one
+        // shape): 32x8x16 in 3D, 32x16 in 2D.  The autotuner's table times
+        // single evaluations, where the tile sets the latency of one
+        // launch; in the batch every launch carries all pairs and the
+        // deeper tile's lower per-item overhead wins (60-frame 2D series:
+        // 1733-1778 pairs/s with 32x16 against 1389-1415 with the tuned
+        // 32x8; the 3D cohort the same either way).
+        std::vector<std::array<int, 3>> level_tile(
+            levels, dim == 3 ? std::array<int, 3>{32, 8, 16} : std::array<int, 3>{32, 16, 1});
         // levels the pairs have left are destroyed on a helper thread while
         // the next passes run.  Their buffers are freed on a stream other
         // than st, ordered after their last use by an event on st: st may be
@@ -790,6 +794,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                         mgr_level *L = nullptr;
                         ckm(mgr_level_create(&d, device, sp, &L));
                         r.made[shift] = L;
+                        const int *tile = level_tile[shift].data();
                         ckm(mgr_level_set_path(L, MGR_PATH_SPLIT, tile[0], tile[1], tile[2]));
                         level_set_images_async(L, src_l.p, ref_l.p);
                         if (refine_grows(dim, csize, ncn)) {
@@ -835,6 +840,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                 for (int w = 0; w < nworkers; ++w)
                     ck(cudaStreamWaitEvent(st, events.e[size_t(w) * levels + shift], 0), "cudaStreamWaitEvent");
             }
+            int *tile = level_tile[shift].data();
             for (int pass = 0; pass < 2; ++pass) {
                 TraceScope tr_lvl("batch: refine+level setup", st);
                 if (pass == 1) {

@@ -13,6 +13,7 @@
 #include "../../include/mgr.h"
 #include "mgr_kernels.hh"
 #include "tables.hh"
+#include "tune.hh"
 
 namespace mgr {
 
@@ -235,23 +236,42 @@ struct mgr_level {
         return a;
     }
 
-    // 3D: the deepest z tile (16, 8, 4) whose warp block fits three to an SM
-    // and whose adjoint block fits in 64 KiB of shared memory (small
+    // whether tile t is compiled in and, in 3D, its warp block fits three to
+    // an SM and its adjoint block fits in 64 KiB of shared memory (small
     // coefficient spacings widen the footprints)
-    void choose_tile3()
+    bool tile_fits(const int t[3]) const
     {
+        if (!tile_supported(d.dim, t[0], t[1], t[2])) return false;
+        if (d.dim == 2) return true;
+        AxisHost hx, hy, hz;
+        build_axis(hx, n[0], nc[0], t[0]);
+        build_axis(hy, n[1], nc[1], t[1]);
+        build_axis(hz, n[2], nc[2], t[2]);
+        const size_t w = (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(12) * 16 * 64) * sizeof(float);
+        const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
+        return w <= 74 * 1024 && adj <= 64 * 1024;
+    }
+
+    // the tile of the autotuner's nearest case (tune.cc) when it fits, else
+    // 32x16 in 2D and in 3D the deepest z tile (16, 8, 4) that fits
+    void choose_tile()
+    {
+        int t[3];
+        if (tuned_tile(d.dim, n, nc, t) && tile_fits(t)) {
+            for (int k = 0; k < 3; ++k) tile[k] = t[k];
+            return;
+        }
+        if (d.dim == 2) {
+            tile[0] = 32;
+            tile[1] = 16;
+            tile[2] = 1;
+            return;
+        }
         static const int tzs[3] = {16, 8, 4};
         for (int k = 0; k < 3; ++k) {
-            tile[0] = 32;
-            tile[1] = 8;
-            tile[2] = tzs[k];
-            AxisHost hx, hy, hz;
-            build_axis(hx, n[0], nc[0], tile[0]);
-            build_axis(hy, n[1], nc[1], tile[1]);
-            build_axis(hz, n[2], nc[2], tile[2]);
-            const size_t w = (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(12) * 16 * 64) * sizeof(float);
-            const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
-            if (w <= 74 * 1024 && adj <= 64 * 1024) return;
+            const int c[3] = {32, 8, tzs[k]};
+            for (int j = 0; j < 3; ++j) tile[j] = c[j];
+            if (tile_fits(c)) return;
         }
     }
 

@@ -87,6 +87,13 @@ class Level:
         t = list(tile) + [0] * (3 - len(tile))
         check(lib().mgr_level_set_path(self.h, p, *t))
 
+    @property
+    def tile(self):
+        """the split path's tile shape (x, y, z)"""
+        t = (ctypes.c_int * 3)()
+        check(lib().mgr_level_tile(self.h, t))
+        return tuple(t)
+
     def set_images(self, src, ref):
         s, r = _f(src), _f(ref)
         assert s.shape == self.shape and r.shape == self.shape
