@@ -54,10 +54,8 @@ BATCH_WORKLOADS = {
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from mia_gb300 import replicas
+    return replicas.env()
 
 
 def make_workload(name, device):
@@ -310,18 +308,30 @@ def measure_batch(name, steps, warmup, device, cpu_seconds=0.0, clocks=None, pro
 
 
 def run_batch(args):
-    """one JSON line for a registration workload (pairs/s)"""
+    """one JSON line for a registration workload (pairs/s); with N ranks,
+    N replicas of the workload, the slowest rank's time counts"""
+    from mia_gb300 import replicas
     ws, rank, local = dist_env()
     import torch
+    replicas.init()
     torch.cuda.set_device(local)
     name = args.workload
     clk = ClockSampler(local)
-    r = measure_batch(name, args.steps, args.warmup, local, 0.0 if args.no_cpu_baseline else args.cpu_seconds,
+    replicas.barrier()
+    r = measure_batch(name, args.steps, args.warmup, local,
+                      0.0 if (args.no_cpu_baseline or rank != 0) else args.cpu_seconds,
                       profile_region=args.profile_region,
                       clocks=clk)
+    replicas.barrier()
+    value, t_max = replicas.whole_job_rate(r["npairs"], r["ms_per_step"] / 1e3, ws,
+                                           device=torch.device("cuda", local))
+    e2e_v, _ = replicas.whole_job_rate(r["npairs"], r["npairs"] / r["e2e"]["value"], ws,
+                                       device=torch.device("cuda", local))
     if rank != 0:
         return 0
-    line = {"metric": METRIC, "value": ws * r["value"], "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+    r["e2e"]["value"] = e2e_v
+    r["ms_per_step"] = t_max * 1e3
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
     line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
@@ -422,10 +432,9 @@ def run_reference_batch(args):
 
 def run_gpu(args):
     import torch
+    from mia_gb300 import replicas
     ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    replicas.init()
     torch.cuda.set_device(local)
     import mia_gb300 as M
     name = args.workload
@@ -443,10 +452,7 @@ def run_gpu(args):
     lv.set_timing(True)
     torch.cuda.synchronize()
 
-    def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = replicas.barrier
 
     for _ in range(args.warmup):
         lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
@@ -466,13 +472,7 @@ def run_gpu(args):
     barrier()
     launches = M.lib().mgr_kernel_launch_count() - launches0
     per = np.array(per)
-    t_step = per[:, 3].mean() / 1e3
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_step], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = ws * N / t_step / 1e6
+    value, t_step = replicas.whole_job_rate(N / 1e6, per[:, 3].mean() / 1e3, ws, device=dev)
 
     # end to end through the C ABI: host (pinned) params in, gradient out
     hp = torch.from_numpy(params).pin_memory().numpy()
@@ -487,12 +487,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         lv.evaluate_total(hp, hg)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_step = float(np.mean(e2e_t))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_step], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
+    e2e_step = replicas.max_over_ranks(float(np.mean(e2e_t)), device=dev)
 
     if rank != 0:
         return 0
