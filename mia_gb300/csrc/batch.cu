@@ -648,14 +648,10 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         const size_t ev_normalized = size_t(nworkers) * levels;
         const size_t ev_retired = ev_normalized + 1;
         // one tile for all pairs and levels (the batch kernels take one
-        // shape): 32x8x16 in 3D, 32x16 in 2D.  The autotuner's table times
-        // single evaluations, where the tile sets the latency of one
-        // launch; in the batch every launch carries all pairs and the
-        // deeper tile's lower per-item overhead wins (60-frame 2D series:
-        // 1733-1778 pairs/s with 32x16 against 1389-1415 with the tuned
-        // 32x8; the 3D cohort the same either way).
-        std::vector<std::array<int, 3>> level_tile(
-            levels, dim == 3 ? std::array<int, 3>{32, 8, 16} : std::array<int, 3>{32, 16, 1});
+        // shape): the registration drivers' tile
+        std::array<int, 3> rt;
+        registration_tile(dim, rt.data());
+        std::vector<std::array<int, 3>> level_tile(levels, rt);
         // levels the pairs have left are destroyed on a helper thread while
         // the next passes run.  Their buffers are freed on a stream other
         // than st, ordered after their last use by an event on st: st may be

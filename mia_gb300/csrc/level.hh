@@ -319,6 +319,19 @@ struct mgr_level {
 };
 
 namespace mgr {
+// The tile of the registration drivers' split path, per pair (register.cu)
+// and batched (batch.cu), so that both run the same kernels in the same
+// order: 32x8x16 in 3D, 32x16 in 2D.  The autotuner's table times single
+// evaluations, where the tile sets the latency of one launch; in the batch
+// every launch carries all pairs and the deeper tile's lower per-item
+// overhead wins (60-frame 2D series: 1733-1778 pairs/s with 32x16 against
+// 1389-1415 with the tuned 32x8; the 3D cohort the same either way).
+inline void registration_tile(int dim, int t[3])
+{
+    t[0] = 32;
+    t[1] = dim == 3 ? 8 : 16;
+    t[2] = dim == 3 ? 16 : 1;
+}
 // mgr_level_set_images_device without the final stream synchronisation
 void level_set_images_async(mgr_level *L, const float *d_src, const float *d_ref);
 // a new coefficient grid (and tile) on a level, images kept

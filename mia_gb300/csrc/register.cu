@@ -93,7 +93,10 @@ double register_pair_device(const mgr_level_desc &full, int levels, const mgr_mi
             TraceScope tr_lvl("pair: level setup", st);
             LevelHandle lv;
             ckm(mgr_level_create(&d, device, st, &lv.h));
-            ckm(mgr_level_set_path(lv.h, path, 0, 0, 0));
+            int t[3];
+            registration_tile(dim, t);
+            if (lv.h->tile_fits(t)) ckm(mgr_level_set_path(lv.h, path, t[0], t[1], t[2]));
+            else ckm(mgr_level_set_path(lv.h, path, 0, 0, 0));
             level_set_images_async(lv.h, src_l.p, ref_l.p);
             tr_lvl.stop();
             TraceScope tr_min("pair: minimizer", st);
