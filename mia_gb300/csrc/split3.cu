@@ -167,6 +167,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     __shared__ float urng[NT3 / 32][6];   // per warp: footprint min / max per component
     __shared__ int boxs[8];               // staged, xs, ylo, zbase, nplanes, span, w4, rows
     __shared__ __align__(8) unsigned long long mbar[RING_N];
+    __shared__ unsigned rdone[RING_N];    // warps done with the ring slot's current plane
     __shared__ bool is_last;
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
@@ -254,8 +255,10 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             Tx[r * 32 + lane] = fwx.x * c[0] + fwx.y * c[1] + fwx.z * c[2] + fwx.w * c[3];
         }
         if (tid == 0) {
-            for (int k = 0; k < RING_N; ++k)
+            for (int k = 0; k < RING_N; ++k) {
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[k])) : "memory");
+                rdone[k] = 0;
+            }
             asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         }
     }
@@ -455,19 +458,30 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         r2 = (inxy && t + 3 < ez) ? __ldg(rin + 3 * nxy) : 0.0f;
         wout += nxy;
         rin += nxy;
-        if (staged) {
-            // plane t is no longer needed: its slot takes plane t + RING_N
-            __syncthreads();
-            if (tid == 0 && ring_ok && t + RING_N < nplanes) {
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                issue_plane(t + RING_N);
-                ++issued;
+        if (staged && t + RING_N < nplanes) {
+            // this warp is done with plane t; the last warp to be done
+            // refills the slot with plane t + RING_N (the warps run apart
+            // by up to the ring's slack instead of meeting at a barrier
+            // every plane)
+            __syncwarp();
+            if (lane == 0) {
+                const int slot = ring_slot(t);
+                __threadfence_block();
+                if (atomicAdd(&rdone[slot], 1u) == unsigned(NT3 / 32 - 1)) {
+                    rdone[slot] = 0;
+                    if (ring_ok) {
+                        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                        issue_plane(t + RING_N);
+                    }
+                }
             }
         }
     }
+    if (staged) __syncthreads();   // every warp is done with the ring
     if (staged && tid == 0) {
         // copies still in flight (only after a wait gave up) are waited for
         // before the block's shared memory is released
+        issued = nplanes;
         while (kwait < issued) {
             if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) break;
             ++kwait;
