@@ -247,7 +247,8 @@ struct mgr_level {
         build_axis(hx, n[0], nc[0], t[0]);
         build_axis(hy, n[1], nc[1], t[1]);
         build_axis(hz, n[2], nc[2], t[2]);
-        const size_t w = (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(12) * 16 * 64) * sizeof(float);
+        const size_t w =
+            (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(WARP_RING_PLANES) * 16 * 64) * sizeof(float);
         const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
         return w <= 74 * 1024 && adj <= 64 * 1024;
     }

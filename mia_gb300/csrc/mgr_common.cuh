@@ -278,6 +278,11 @@ struct Axis {
 // longest per-axis list of tiles whose adjoint footprint holds a coefficient
 // that the 3D gather reads from the tables (longer lists take a slower path)
 constexpr int GATHER_LMAX = 24;
+// planes of the 3D warp kernel's shared-memory tap ring (split3.cu); the
+// tile-fit rule (mgr_level::tile_fits) counts them.  12 keeps three warp
+// blocks per SM at the usual spacings (14 measured slower: 2 blocks per SM
+// at rate 5)
+constexpr int WARP_RING_PLANES = 12;
 
 // scalars written by the cost finalisation (double[16])
 enum {

@@ -92,7 +92,7 @@ __device__ __noinline__ float taps3_global(const EvalArgs &a, float px, float py
 // banks, so a warp whose lanes straddle two rows or planes reads without
 // bank conflicts).  A tile whose taps do not fit (large variation of the
 // displacement over the tile) reads them from global memory instead.
-constexpr int RING_N = 12;
+constexpr int RING_N = WARP_RING_PLANES;
 constexpr int RING_Y = 16;
 constexpr int RING_X = 64;
 constexpr int RING_PLANE = RING_Y * RING_X;
