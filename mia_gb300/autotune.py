@@ -26,11 +26,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "tiles.json")
 
-# image size (x, y[, z]), rate, cost: the 3D eval benchmark sizes, the
+# image size (x, y[, z]), rate, cost: the 3D eval benchmark workloads, the
 # levels of the 3D cohort (full, 1/2, 1/4 of ~160x176x144), denser and
 # coarser grids, 2D perfusion frames (series sizes) and large slices
 CASES = [
     dict(size=(192, 192, 128), rate=8.0, cost="ssd"),
+    dict(size=(256, 256, 256), rate=5.0, cost="ncc"),
     dict(size=(256, 256, 256), rate=8.0, cost="ncc"),
     dict(size=(160, 176, 144), rate=8.0, cost="ncc"),
     dict(size=(80, 88, 72), rate=8.0, cost="ncc"),
@@ -43,7 +44,7 @@ CASES = [
     dict(size=(512, 512), rate=8.0, cost="ssd"),
     dict(size=(1024, 1024), rate=16.0, cost="ssd"),
 ]
-TILES3 = [(32, 8, 16), (32, 8, 8), (32, 8, 4)]
+TILES3 = [(32, 8, 32), (32, 8, 16), (32, 8, 8), (32, 8, 4)]
 TILES2 = [(32, 8, 1), (32, 16, 1), (64, 8, 1), (64, 16, 1), (32, 32, 1)]
 
 

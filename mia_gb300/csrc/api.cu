@@ -580,7 +580,7 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
                     tile_z > 0 ? tile_z : lvl->tile[2]};
         if (lvl->d.dim == 2) t[2] = 1;
         if (!tile_supported(lvl->d.dim, t[0], t[1], t[2]))
-            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x16, 32x8x8, 32x8x4; "
+            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x32, 32x8x16, 32x8x8, 32x8x4; "
                                         "2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
         bool changed = false;
         for (int k = 0; k < 3; ++k)

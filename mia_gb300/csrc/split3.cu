@@ -1092,7 +1092,7 @@ size_t split3_smem(const EvalArgs &a, int which)
 
 bool tile_supported3(int tx, int ty, int tz)
 {
-    return tx == TX3 && ty == TY3 && (tz == 4 || tz == 8 || tz == 16);
+    return tx == TX3 && ty == TY3 && (tz == 4 || tz == 8 || tz == 16 || tz == 32);
 }
 
 namespace {
@@ -1137,6 +1137,7 @@ void launch_warp3(const EvalArgs &a, cudaStream_t st)
     switch (a.ax[2].t) {
     case 4: launch_warp3_z<4>(a, sm, st); break;
     case 8: launch_warp3_z<8>(a, sm, st); break;
+    case 32: launch_warp3_z<32>(a, sm, st); break;
     default: launch_warp3_z<16>(a, sm, st); break;
     }
     count_launch();
@@ -1148,6 +1149,7 @@ void launch_adjoint3(const EvalArgs &a, cudaStream_t st)
     switch (a.ax[2].t) {
     case 4: launch_adjoint3_z<4>(a, sm, st); break;
     case 8: launch_adjoint3_z<8>(a, sm, st); break;
+    case 32: launch_adjoint3_z<32>(a, sm, st); break;
     default: launch_adjoint3_z<16>(a, sm, st); break;
     }
     count_launch();
@@ -1169,6 +1171,7 @@ void prepare_split3_batch(int tz, size_t sm_warp, size_t sm_adj)
     switch (tz) {
     case 4: prepare3_z<4>(sm_warp, sm_adj); break;
     case 8: prepare3_z<8>(sm_warp, sm_adj); break;
+    case 32: prepare3_z<32>(sm_warp, sm_adj); break;
     default: prepare3_z<16>(sm_warp, sm_adj); break;
     }
 }
@@ -1179,6 +1182,7 @@ void launch_split3_batch(int tz, const EvalArgs *args, const int2 *items, int ni
     switch (tz) {
     case 4: batch3_z<4>(args, items, nitems, active, sm, which, st); break;
     case 8: batch3_z<8>(args, items, nitems, active, sm, which, st); break;
+    case 32: batch3_z<32>(args, items, nitems, active, sm, which, st); break;
     default: batch3_z<16>(args, items, nitems, active, sm, which, st); break;
     }
     count_launch();
