@@ -182,6 +182,99 @@ def cpu_baseline(w, mov, ref, params, seconds, threads):
     return N * n / dt / 1e6, n, dt, res
 
 
+def time_evals(lv, p_d, g_d, c_d, flush, steps, warmup=2):
+    """device ms of one cost+gradient evaluation (the level's own events,
+    L2 flushed before each), mean over `steps`"""
+    import torch
+    lv.set_timing(True)
+    for _ in range(warmup):
+        lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
+    lv.sync()
+    per = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
+        lv.sync()
+        per.append(lv.kernel_times()[3])
+    return float(np.mean(per))
+
+
+def split_vs_plain(lv, p_d, g_d, c_d, flush, steps, N):
+    """the split (fused forward + adjoint) kernels against the plain
+    separate init_grid / warp / force / translate kernels, same GPU, same
+    inputs"""
+    t_split = time_evals(lv, p_d, g_d, c_d, flush, steps)
+    lv.set_path("plain")
+    t_plain = time_evals(lv, p_d, g_d, c_d, flush, steps)
+    lv.set_path("split")
+    return {"split_ms": t_split, "plain_ms": t_plain, "plain_value": N / t_plain / 1e3, "unit": "Mvoxel/s",
+            "speedup_split_vs_plain": t_plain / t_split}
+
+
+def fd_check(w, mov, ref, params, lv, ref_grads, threads, ncoef=64, h=1e-3, seed=7):
+    """the gradient against FP64 central finite differences of the FP64
+    oracle's total cost on `ncoef` random coefficients; the reference's own
+    gradient (the oracle at reference precision) against the same
+    differences for comparison: the reference's image gradient takes the
+    warped image's derivative by central differences, so neither equals FD
+    exactly"""
+    from oracle import oracle as O
+    o64 = O.Level(w["size"], rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], precision=O.PREC_F64,
+                  threads=threads)
+    o64.set_images(mov, ref)
+    _, _, gi, gp, _ = lv.evaluate(params)
+    d_gpu = gi - gp   # the penalty gradient carries the reference's sign (-weight * gradient)
+    ogi, ogp = ref_grads
+    d_ref = ogi - ogp
+    idx = np.random.default_rng(seed).choice(params.size, ncoef, replace=False)
+    fd = np.empty(ncoef)
+    t0 = time.perf_counter()
+    for k, i in enumerate(idx):
+        pp, pm = params.copy(), params.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd[k] = (sum(o64.value(pp)) - sum(o64.value(pm))) / (2 * h)
+    del o64
+    nrm = float(np.linalg.norm(fd))
+    return {"coefficients": ncoef, "h": h, "seed": seed, "seconds": time.perf_counter() - t0,
+            "rel_l2_gpu_vs_fd": float(np.linalg.norm(d_gpu[idx] - fd) / nrm),
+            "rel_l2_reference_gradient_vs_fd": float(np.linalg.norm(d_ref[idx] - fd) / nrm),
+            "rel_l2_gpu_vs_reference_gradient": float(np.linalg.norm(d_gpu[idx] - d_ref[idx]) /
+                                                      np.linalg.norm(d_ref[idx]))}
+
+
+def ncc_256_summary(device, flush, threads):
+    """256^3 NCC with bias field: split against plain kernels on this GPU,
+    error against the oracle at reference precision"""
+    import torch
+    import mia_gb300 as M
+    from oracle import oracle as O
+    name = "3d_ncc_256x256x256"
+    w, mov, ref, params = make_workload(name, device)
+    size = w["size"]
+    N = int(np.prod(size))
+    lv = M.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], device=device)
+    lv.set_images(mov, ref)
+    dev = torch.device("cuda", device)
+    p_d = torch.from_numpy(params).to(dev)
+    g_d = torch.empty(lv.nparams, dtype=torch.float64, device=dev)
+    c_d = torch.empty(2, dtype=torch.float64, device=dev)
+    out = {"workload": name, "size": list(size), "rate": w["rate"], "tile": list(lv.tile)}
+    out.update(split_vs_plain(lv, p_d, g_d, c_d, flush, 5, N))
+    out["value"] = N / out["split_ms"] / 1e3
+    ci, cp, gi, gp, _ = lv.evaluate(params)
+    o = O.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], threads=threads)
+    o.set_images(mov, ref)
+    oi, op, ogi, ogp = o.evaluate(params)
+    out["parity"] = {"cost_image_rel": abs(ci - oi) / abs(oi), "cost_penalty_rel": abs(cp - op) / abs(op),
+                     "grad_image_rel_l2": float(np.linalg.norm(gi - ogi) / np.linalg.norm(ogi)),
+                     "grad_penalty_rel_l2": float(np.linalg.norm(gp - ogp) / np.linalg.norm(ogp)),
+                     "against": "oracle, reference precision"}
+    lv.close()
+    return out
+
+
 def make_pairs(name, device):
     """Host (moving, reference) pairs of a registration workload; the random
     deformations are applied with this library's warp on `device`."""
@@ -519,6 +612,8 @@ def run_gpu(args):
         "eval_roofline": eval_roof,
         "clocks": clk.summary(),
     }
+    if ws == 1:
+        line["split_vs_plain"] = split_vs_plain(lv, p_d, g_d, c_d, flush, max(3, min(args.steps, 10)), N)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, n, dt, res = cpu_baseline(w, mov, ref, params, args.cpu_seconds, threads)
@@ -531,6 +626,11 @@ def run_gpu(args):
             "grad_image_rel_l2": float(np.linalg.norm(gi - ogi) / np.linalg.norm(ogi)),
             "grad_penalty_rel_l2": float(np.linalg.norm(gp - ogp) / np.linalg.norm(ogp)),
             "against": "oracle, reference precision"}
+        line["fd_check"] = fd_check(w, mov, ref, params, lv, (ogi, ogp), threads)
+        if name == "3d_ssd_192x192x128" and not args.no_batched:
+            # the 3D NCC configuration: split vs plain kernels and parity
+            lv.close()
+            line["ncc_256"] = ncc_256_summary(local, flush, threads)
     if ws == 1 and not args.no_batched:
         # the registration workloads (pairs/s): batched path against the
         # per-pair GPU driver on the same pairs
