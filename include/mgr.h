@@ -261,6 +261,26 @@ mgr_status mgr_refine_coefficients(int dim, const int nc_old[3], const int nc_ne
 mgr_status mgr_refine_coefficients_device(int dim, const int nc_old[3], const int nc_new[3], const double *d_in,
                                           double *d_out, int *grown, void *stream);
 
+/* Replaces: the `xml` transformation IO plugin (mia/3d/transio/xml.cc:55-73,
+   mia/2d/transio/xml.cc; fields as mia/3d/transio/serialization.hh:35-83):
+   writes a spline transformation — the creator string (e.g.
+   "spline:rate=8"), the image size, the attributes (name/value strings) and
+   the parameters (prod(csize) * dim, interleaved, x fastest) — as a Boost
+   XML archive layout; the coefficient grid is stored as the attribute
+   "csize".  Host code only. */
+mgr_status mgr_transform_save(const char *path, int dim, const int size[3], const int csize[3],
+                              const char *creator, const double *params, size_t nparams,
+                              const char *const *attr_names, const char *const *attr_values, int nattr);
+
+/* Reads what mgr_transform_save wrote.  Writes dim, size, csize,
+   *nparams; the creator string and the attributes ("name\tvalue\n" lines,
+   csize excluded) when their buffers are given; the parameters when
+   `params` is given (params_cap >= *nparams).  Call with params = NULL to
+   learn *nparams first. */
+mgr_status mgr_transform_load(const char *path, int *dim, int size[3], int csize[3], char *creator,
+                              size_t creator_cap, char *attrs, size_t attrs_cap, double *params,
+                              size_t params_cap, size_t *nparams);
+
 /* Wait for all work queued on the level's stream. */
 mgr_status mgr_level_sync(mgr_level *lvl);
 

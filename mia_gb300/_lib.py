@@ -46,6 +46,12 @@ SIGNATURES = {
                                                  ctypes.c_int, _vp, _vp, _ip, _dp, _ip]),
     "mgr_scale_image": (ctypes.c_int, [ctypes.c_int, _ip, _fp, _ip, _fp, ctypes.c_int]),
     "mgr_level_tile": (ctypes.c_int, [_vp, _ip]),
+    "mgr_transform_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, ctypes.c_char_p, _dp,
+                                          ctypes.c_size_t, ctypes.POINTER(ctypes.c_char_p),
+                                          ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]),
+    "mgr_transform_load": (ctypes.c_int, [ctypes.c_char_p, _ip, _ip, _ip, ctypes.c_char_p, ctypes.c_size_t,
+                                          ctypes.c_char_p, ctypes.c_size_t, _dp, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
     "mgr_refine_coefficients": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, _ip]),
     "mgr_refine_coefficients_device": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _vp, _vp, _ip, _vp]),
     "mgr_normalize_pair": (ctypes.c_int, [_fp, _fp, ctypes.c_size_t, _fp, _fp, _dp, _dp, _ip, ctypes.c_int]),

@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "libmgr.so")
 BUILD = os.path.join(HERE, "_build")
 
 CU_SOURCES = ["api.cu", "eval.cu", "split.cu", "split3.cu", "gather.cu", "prefilter.cu", "noalloc.cu", "pyramid.cu", "register.cu", "batch.cu", "refine.cu"]
-CXX_SOURCES = ["tables.cc", "driver.cc", "tune.cc"]
+CXX_SOURCES = ["tables.cc", "driver.cc", "tune.cc", "transio.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 TILES_JSON = os.path.join(HERE, "tiles.json")
 TILE_TABLE = os.path.join(BUILD, "tile_table.inc")

@@ -87,6 +87,58 @@ def refine_coefficients_device(d_params, d_out, nc_old, nc_new, stream=0):
     return bool(grown.value)
 
 
+def save_transform(path, size_xyz, csize, params, rate=None, creator=None, attributes=None):
+    """write a spline transformation (mgr_transform_save): image size
+    (x, y[, z]), coefficient grid, parameters; the creator string defaults
+    to spline:rate=<rate> (the registration's rate; without one, the mean
+    knot spacing of the grid)"""
+    dim = len(size_xyz)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    if creator is None:
+        if rate is None:
+            rate = np.mean([(n - 1) / max(c - 3, 1) for n, c in zip(size_xyz, csize)])
+        creator = "spline:rate=%g" % rate
+    attributes = dict(attributes or {})
+    names = (ctypes.c_char_p * max(1, len(attributes)))(*[k.encode() for k in attributes])
+    values = (ctypes.c_char_p * max(1, len(attributes)))(*[str(v).encode() for v in attributes.values()])
+    sz = (ctypes.c_int * 3)(*(list(size_xyz) + [1] * (3 - dim)))
+    cs = (ctypes.c_int * 3)(*(list(csize) + [1] * (3 - dim)))
+    check(lib().mgr_transform_save(str(path).encode(), dim, sz, cs, creator.encode(), p.ctypes.data_as(_dp), p.size,
+                                   names, values, len(attributes)))
+
+
+def load_transform(path):
+    """read what save_transform wrote: dict(dim, size, csize, creator,
+    attributes, params)"""
+    dim, n = ctypes.c_int(), ctypes.c_size_t()
+    sz, cs = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    check(lib().mgr_transform_load(str(path).encode(), ctypes.byref(dim), sz, cs, None, 0, None, 0, None, 0,
+                                   ctypes.byref(n)))
+    params = np.empty(n.value)
+    creator = ctypes.create_string_buffer(4096)
+    attrs = ctypes.create_string_buffer(1 << 16)
+    check(lib().mgr_transform_load(str(path).encode(), ctypes.byref(dim), sz, cs, creator, len(creator), attrs,
+                                   len(attrs), params.ctypes.data_as(_dp), params.size, ctypes.byref(n)))
+    d = dim.value
+    attributes = dict(line.split("\t", 1) for line in attrs.value.decode().splitlines() if line)
+    return dict(dim=d, size=tuple(sz[:d]), csize=tuple(cs[:d]), creator=creator.value.decode(),
+                attributes=attributes, params=params)
+
+
+def warp_image(img, csize, params, device=0):
+    """the image (numpy [z, y, x], full size) transformed by the spline
+    transformation with coefficient grid csize: the registration programs'
+    output image (bspline:d=3 interpolation, mirror boundary, clamp)"""
+    from .level import Level
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    lv = Level(a.shape[::-1], csize=tuple(csize), device=device)
+    try:
+        lv.set_images(a, a)
+        return lv.warp(params)
+    finally:
+        lv.close()
+
+
 def normalize_pair(src, ref, device=0):
     s = np.ascontiguousarray(src, dtype=np.float32)
     r = np.ascontiguousarray(ref, dtype=np.float32)

@@ -82,3 +82,24 @@ def test_register_3d_matches_oracle(cost, kind):
     assert csg == cso
     assert abs(fg - fo) <= FINAL_COST_RTOL * abs(fo), (fg, fo)
     assert np.linalg.norm(pg - po) <= 1e-3 * np.linalg.norm(po)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_registered_transform_saved_loaded_and_applied(tmp_path, dim):
+    """the output of a registration program: the transformation written with
+    the transformation IO, read back, and the moving image warped with it"""
+    from mia_gb300 import registration as R
+    mov, ref = _pair2d(7) if dim == 2 else _pair3d(8)
+    rate = 16.0 if dim == 2 else 8.0
+    mz = R.minimizer("gsl", maxiter=20, step=0.1)
+    params, csize, cost, _ = R.register_pair(mov, ref, rate, 1, mz, cost="ssd", penalty_weight=10.0)
+    size = mov.shape[::-1]
+    f = tmp_path / ("reg.x%ddt" % dim)
+    R.save_transform(f, size, csize, params, rate=rate)
+    t = R.load_transform(f)
+    assert t["csize"] == tuple(csize) and t["creator"] == "spline:rate=%g" % rate
+    warped = R.warp_image(mov, t["csize"], t["params"])
+    np.testing.assert_array_equal(warped, R.warp_image(mov, csize, params))
+    before = float(np.sum((mov.astype(np.float64) - ref) ** 2))
+    after = float(np.sum((warped.astype(np.float64) - ref) ** 2))
+    assert after < 0.8 * before
