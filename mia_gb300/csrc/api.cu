@@ -376,8 +376,18 @@ static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref
 
 static void upload_params(mgr_level *L, const double *params)
 {
-    for (size_t i = 0; i < L->nparams; ++i)
-        if (!std::isfinite(params[i])) throw std::invalid_argument("parameters must be finite");
+    // x - x is 0 for finite x and NaN otherwise: eight independent sums
+    // (no branch per value, the loop vectorises) are 0 exactly when every
+    // parameter is finite
+    const size_t n = L->nparams;
+    double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8)
+        for (int k = 0; k < 8; ++k) acc[k] += params[i + k] - params[i + k];
+    for (; i < n; ++i) acc[0] += params[i] - params[i];
+    double all = 0.0;
+    for (double v : acc) all += v;
+    if (all != 0.0) throw std::invalid_argument("parameters must be finite");
     ck(cudaMemcpyAsync(L->params.p, params, L->nparams * sizeof(double), cudaMemcpyHostToDevice, L->stream),
        "params H2D");
 }
@@ -477,14 +487,17 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
         if (grad_image) ck(cudaMemcpyAsync(grad_image, lvl->grad_image.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
         if (grad_penalty)
             ck(cudaMemcpyAsync(grad_penalty, lvl->grad_penalty.p, bytes, cudaMemcpyDeviceToHost, st), "D2H");
-        double c[2];
-        ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
-        unsigned flag = 0;
-        read_status_flag(lvl, &flag);
+        // costs and status flag into the level's pinned buffer: asynchronous
+        // copies, one synchronisation
+        double *hc = lvl->host_small();
+        ck(cudaMemcpyAsync(hc, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        ck(cudaMemcpyAsync(hc + 2, lvl->counters.p + 6, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "D2H");
         ck(cudaStreamSynchronize(st), "evaluate sync");
+        unsigned flag;
+        std::memcpy(&flag, hc + 2, sizeof flag);
         throw_if_flagged(lvl, flag);
-        if (cost_image) *cost_image = c[0];
-        if (cost_penalty) *cost_penalty = c[1];
+        if (cost_image) *cost_image = hc[0];
+        if (cost_penalty) *cost_penalty = hc[1];
     });
 }
 
@@ -499,14 +512,16 @@ mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_im
         launch_warp(a, lvl->stream);
         launch_gather(a, 0, lvl->stream);
         check_launch("value kernels");
-        double c[2];
-        ck(cudaMemcpyAsync(c, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
-        unsigned flag = 0;
-        read_status_flag(lvl, &flag);
+        double *hc = lvl->host_small();
+        ck(cudaMemcpyAsync(hc, lvl->costs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        ck(cudaMemcpyAsync(hc + 2, lvl->counters.p + 6, sizeof(unsigned), cudaMemcpyDeviceToHost, lvl->stream),
+           "D2H");
         ck(cudaStreamSynchronize(lvl->stream), "value sync");
+        unsigned flag;
+        std::memcpy(&flag, hc + 2, sizeof flag);
         throw_if_flagged(lvl, flag);
-        if (cost_image) *cost_image = c[0];
-        if (cost_penalty) *cost_penalty = c[1];
+        if (cost_image) *cost_image = hc[0];
+        if (cost_penalty) *cost_penalty = hc[1];
     });
 }
 

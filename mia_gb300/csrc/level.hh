@@ -180,10 +180,19 @@ struct mgr_level {
     {
         if (timing) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");
     }
+    // 4 doubles of pinned host memory for small read-backs (costs, status)
+    double *host_small_p = nullptr;
+    double *host_small()
+    {
+        if (!host_small_p) ck(cudaMallocHost(reinterpret_cast<void **>(&host_small_p), 4 * sizeof(double)),
+                              "cudaMallocHost");
+        return host_small_p;
+    }
     ~mgr_level()
     {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
+        if (host_small_p) cudaFreeHost(host_small_p);
     }
 
     // a level made on another level's images (the refine pass of a batched

@@ -258,3 +258,26 @@ def test_penalty_gradient_is_minus_fd():
         pm = p.copy(); pm[i] -= h
         fd = (o64.value(pp)[1] - o64.value(pm)[1]) / (2 * h)
         assert abs(gp[i] + fd) <= 1e-3 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("where", [0, 17, 48, 49])
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_non_finite_parameters_are_rejected(where, bad):
+    """evaluate and value refuse parameters that are not finite (any slot,
+    the last ones included) and the level keeps working"""
+    import mia_gb300 as M
+    from mia_gb300 import _lib
+    lv = M.Level((30, 26), csize=(5, 5), cost="ssd", penalty_weight=1.0)
+    a, b = make_pair((26, 30), 3)
+    lv.set_images(a, b)
+    p = np.zeros(lv.nparams)
+    assert lv.nparams == 50
+    p[where] = bad
+    with pytest.raises(_lib.MgrError) as e:
+        lv.evaluate(p)
+    assert e.value.status == _lib.MGR_ERR_ARG
+    with pytest.raises(_lib.MgrError):
+        lv.value(p)
+    p[where] = 0.0
+    ci, cp, gi, gp, gt = lv.evaluate(p)
+    assert np.isfinite(ci) and np.all(np.isfinite(gt))
