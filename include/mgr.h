@@ -61,6 +61,10 @@ typedef struct {
     double pen_div;      /* divcurl `div` */
     double pen_curl;     /* divcurl `curl` */
     int    pen_norm;     /* divcurl `norm` (divide by the image volume) */
+    int    pen_corrected;/* 0: the penalty gradient as the reference returns it,
+                            -weight * gradient (mia/3d/splinetransformpenalty.cc:
+                            60-71); 1: +weight * gradient, the derivative of the
+                            penalty value */
 } mgr_level_desc;
 
 typedef struct mgr_level mgr_level;

@@ -73,6 +73,7 @@ class LevelDesc(ctypes.Structure):
         ("pen_div", ctypes.c_double),
         ("pen_curl", ctypes.c_double),
         ("pen_norm", ctypes.c_int),
+        ("pen_corrected", ctypes.c_int),
     ]
 
 

@@ -143,7 +143,7 @@ __device__ __forceinline__ void gather_body(const EvalArgs &a, int with_gradient
                 }
                 pval = v;
 #pragma unroll
-                for (int k = 0; k < D; ++k) gp[k] = -a.pen_weight * double(G[k]);
+                for (int k = 0; k < D; ++k) gp[k] = (a.pen_grad_sign * a.pen_weight) * double(G[k]);
             }
             if (with_gradient) {
 #pragma unroll

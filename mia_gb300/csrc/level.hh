@@ -232,6 +232,7 @@ struct mgr_level {
         a.has_penalty = d.has_penalty;
         double prod = double(d.size[0]) * d.size[1] * (d.dim == 3 ? d.size[2] : 1);
         a.pen_weight = d.pen_norm ? d.pen_weight / double(float(prod)) : d.pen_weight;
+        a.pen_grad_sign = d.pen_corrected ? 1.0 : -1.0;
         a.pen_equal_w = d.pen_div == d.pen_curl;
         a.ptable = ptable.p;
         a.pen_rowptr = pen_rowptr.p;

@@ -60,6 +60,7 @@ struct EvalArgs {
     // penalty
     int has_penalty;
     double pen_weight;     // effective weight (norm already applied)
+    double pen_grad_sign;  // -1: the reference's penalty gradient sign, +1: corrected
     int pen_equal_w;       // div == curl (multiply skips the cross terms)
     const float *ptable;   // 3D: 9x9x9 cells x 6 floats (xx, xy, yy, yz, zz, xz)
     const int *pen_rowptr; // 2D: CSR rows of the boundary-clipped matrix

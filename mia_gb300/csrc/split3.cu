@@ -922,7 +922,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 v9[k] = t;
             }
             float gp[3] = {0.0f, 0.0f, 0.0f};
-            const float pw = float(a.pen_weight), cw = float(a.cost_weight);
+            const float pw = float(a.pen_grad_sign * a.pen_weight), cw = float(a.cost_weight);
             if (a.has_penalty) {
                 const float ci0 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].x;
                 const float ci1 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].y;
@@ -931,9 +931,9 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                     pval = ci0 * v9[0] + ci0 * v9[1] + ci1 * v9[2] + ci1 * v9[3] + ci2 * v9[4] + ci2 * v9[5];
                 else
                     pval = ci0 * v9[0] + ci1 * v9[2] + ci2 * v9[4] + ci0 * v9[1] + ci0 * v9[6] + ci1 * v9[3];
-                gp[0] = -pw * (v9[6] + (2.0f * v9[0] + v9[1]));
-                gp[1] = -pw * (v9[7] + (2.0f * v9[2] + v9[3]));
-                gp[2] = -pw * (v9[8] + (2.0f * v9[4] + v9[5]));
+                gp[0] = pw * (v9[6] + (2.0f * v9[0] + v9[1]));
+                gp[1] = pw * (v9[7] + (2.0f * v9[2] + v9[3]));
+                gp[2] = pw * (v9[8] + (2.0f * v9[4] + v9[5]));
             }
             if (with_gradient) {
 #pragma unroll

@@ -37,10 +37,13 @@ class Level:
     ssd_norm      ssd `norm`
     cost_weight   image full-cost `weight`
     penalty_weight  divcurl `weight` (None: no penalty); div/curl/penalty_norm
+    penalty_corrected  the penalty gradient as +weight * gradient instead of
+                  the reference's -weight * gradient
     """
 
     def __init__(self, size_xyz, rate=None, csize=None, cost="ssd", ssd_norm=False, cost_weight=1.0,
-                 penalty_weight=None, div=1.0, curl=1.0, penalty_norm=False, device=0, stream=None):
+                 penalty_weight=None, div=1.0, curl=1.0, penalty_norm=False, penalty_corrected=False, device=0,
+                 stream=None):
         d = _lib.LevelDesc()
         d.dim = len(size_xyz)
         d.size = (ctypes.c_int * 3)(*(list(size_xyz) + [1] * (3 - d.dim)))
@@ -55,6 +58,7 @@ class Level:
         d.has_penalty = int(penalty_weight is not None)
         d.pen_weight = float(penalty_weight or 0.0)
         d.pen_div, d.pen_curl, d.pen_norm = float(div), float(curl), int(penalty_norm)
+        d.pen_corrected = int(penalty_corrected)
         self.desc = d
         self.dim = d.dim
         self.size = tuple(size_xyz)

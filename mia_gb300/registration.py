@@ -17,7 +17,7 @@ _fp = ctypes.POINTER(ctypes.c_float)
 
 
 def level_desc(size_xyz, rate, cost="ssd", penalty_weight=None, div=1.0, curl=1.0, ssd_norm=False,
-               cost_weight=1.0, penalty_norm=False):
+               cost_weight=1.0, penalty_norm=False, penalty_corrected=False):
     d = _lib.LevelDesc()
     d.dim = len(size_xyz)
     d.size = (ctypes.c_int * 3)(*(list(size_xyz) + [1] * (3 - d.dim)))
@@ -29,6 +29,7 @@ def level_desc(size_xyz, rate, cost="ssd", penalty_weight=None, div=1.0, curl=1.
     d.has_penalty = int(penalty_weight is not None)
     d.pen_weight = float(penalty_weight or 0.0)
     d.pen_div, d.pen_curl, d.pen_norm = float(div), float(curl), int(penalty_norm)
+    d.pen_corrected = int(penalty_corrected)
     return d
 
 

@@ -281,3 +281,32 @@ def test_non_finite_parameters_are_rejected(where, bad):
     p[where] = 0.0
     ci, cp, gi, gp, gt = lv.evaluate(p)
     assert np.isfinite(ci) and np.all(np.isfinite(gt))
+
+
+@pytest.mark.parametrize("size", [(24, 24, 24), (40, 36)])
+def test_corrected_penalty_gradient_is_plus_fd(size):
+    """pen_corrected: the penalty gradient with the derivative's sign (the
+    default keeps the reference's -weight * gradient); nothing else changes"""
+    import mia_gb300 as M
+    from mia_gb300 import synth
+    kw = dict(rate=4.0, cost="ssd", penalty_weight=10.0)
+    g = M.Level(size, **kw)
+    gc = M.Level(size, penalty_corrected=True, **kw)
+    o64 = O.Level(size, precision=O.PREC_F64, **kw)
+    a, b = make_pair(size[::-1], 5)
+    for lv in (g, gc, o64):
+        lv.set_images(a, b)
+    p = synth.smooth_params(g.csize, 1.0, seed=9)
+    ci, cp, gi, gp, gt = g.evaluate(p)
+    cic, cpc, gic, gpc, gtc = gc.evaluate(p)
+    assert (ci, cp) == (cic, cpc)
+    np.testing.assert_array_equal(gi, gic)
+    np.testing.assert_array_equal(gpc, -gp)
+    np.testing.assert_array_equal(gtc, gic + gpc)
+    rng = np.random.default_rng(2)
+    h = 1e-4
+    for i in rng.choice(p.size, 12, replace=False):
+        pp = p.copy(); pp[i] += h
+        pm = p.copy(); pm[i] -= h
+        fd = (o64.value(pp)[1] - o64.value(pm)[1]) / (2 * h)
+        assert abs(gpc[i] - fd) <= 1e-3 * max(1.0, abs(fd))
