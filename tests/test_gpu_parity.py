@@ -310,3 +310,41 @@ def test_corrected_penalty_gradient_is_plus_fd(size):
         pm = p.copy(); pm[i] -= h
         fd = (o64.value(pp)[1] - o64.value(pm)[1]) / (2 * h)
         assert abs(gpc[i] - fd) <= 1e-3 * max(1.0, abs(fd))
+
+
+def test_levels_evaluated_concurrently_from_host_threads():
+    """one level per registration, each on its own stream: levels used from
+    several host threads at once give the results of serial use"""
+    import threading
+
+    import mia_gb300 as M
+    from mia_gb300 import synth
+    cases = [((36, 32, 28), "ssd"), ((30, 34, 26), "ncc"), ((64, 48), "ssd"), ((40, 44, 36), "ssd")]
+    levels, params = [], []
+    for k, (size, cost) in enumerate(cases):
+        lv = M.Level(size, rate=5.0, cost=cost, penalty_weight=2.0)
+        a, b = make_pair(size[::-1], 30 + k, ncc=cost == "ncc")
+        lv.set_images(a, b)
+        levels.append(lv)
+        params.append(synth.smooth_params(lv.csize, 1.0, seed=40 + k))
+    serial = [[lv.evaluate(p) for _ in range(3)] for lv, p in zip(levels, params)]
+    out = [None] * len(levels)
+    errors = []
+
+    def run(k):
+        try:
+            out[k] = [levels[k].evaluate(params[k]) for _ in range(3)]
+        except Exception as e:   # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(len(levels))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    for s, c in zip(serial, out):
+        for rs, rc in zip(s, c):
+            assert rs[0] == rc[0] and rs[1] == rc[1]
+            for a_, b_ in zip(rs[2:], rc[2:]):
+                np.testing.assert_array_equal(a_, b_)
