@@ -696,8 +696,6 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             if (!images_on_device) {
                 r->src.alloc(n, st);
                 r->ref.alloc(n, st);
-                ck(cudaMemcpyAsync(r->src.p, srcs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
-                ck(cudaMemcpyAsync(r->ref.p, refs[p], n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
                 in_src[p] = r->src.p;
                 in_ref[p] = r->ref.p;
             }
@@ -705,6 +703,21 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             out_ref[p] = r->ref_n.p;
             nvox[p] = n;
             pairs.push_back(std::move(r));
+        }
+        if (!images_on_device) {
+            // host images: the copies from pageable memory are staged by the
+            // calling thread, so the pairs are uploaded from several host
+            // threads, each on its own per-thread stream
+            ck(cudaStreamSynchronize(st), "sync");   // (the buffers were allocated in st's order)
+            parallel_pairs(size_t(npairs), [&](size_t p) {
+                ck(cudaSetDevice(device), "cudaSetDevice");
+                const size_t bytes = nvox[p] * sizeof(float);
+                ck(cudaMemcpyAsync(pairs[p]->src.p, srcs[p], bytes, cudaMemcpyHostToDevice, cudaStreamPerThread),
+                   "H2D");
+                ck(cudaMemcpyAsync(pairs[p]->ref.p, refs[p], bytes, cudaMemcpyHostToDevice, cudaStreamPerThread),
+                   "H2D");
+                ck(cudaStreamSynchronize(cudaStreamPerThread), "H2D sync");
+            });
         }
         const std::vector<char> varied = normalize_pairs(in_src, in_ref, nvox, out_src, out_ref, st);
         for (int p = 0; p < npairs; ++p) {
