@@ -15,6 +15,8 @@ namespace mgr {
 // graph it pauses its own counting (count_launch_pause), and the graph's
 // launches are counted when it runs
 void count_launch(unsigned n = 1);
+// SMs of the current device (cached per device, thread-safe)
+int device_sm_count();
 void count_launch_pause(bool paused);
 
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);

@@ -142,13 +142,7 @@ static int lines_per_block(int n, int lines_total, int blocks_per_line_group)
 {
     int lb = 64;
     while (lb > 1 && size_t(lb) * (n | 1) * sizeof(float) > 64 * 1024) lb >>= 1;
-    static int nsm = 0;
-    if (nsm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm <= 0) nsm = 1;
-    }
+    const int nsm = device_sm_count();
     while (lb > 8 && size_t((lines_total + lb - 1) / lb) * blocks_per_line_group < size_t(2 * nsm)) lb >>= 1;
     return lb;
 }
@@ -156,11 +150,8 @@ static int lines_per_block(int n, int lines_total, int blocks_per_line_group)
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st)
 {
     if (dim == 2) nz = 1;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_prefilter_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
-    }
+    // (a per-device setting: set on every call, once per level)
+    cudaFuncSetAttribute(k_prefilter_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     {
         const int nlines = ny * nz;
         const int lb = lines_per_block(nx, nlines, 1);

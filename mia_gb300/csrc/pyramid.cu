@@ -14,6 +14,7 @@
 //   filters in double; here the lines are filtered in float (FP64 runs at a
 //   small fraction of the FP32 rate on this GPU), which moves the result by
 //   a few float ulp: the parity tests bound it at 1e-5 of the image maximum.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +27,21 @@
 #include "pyramid.hh"
 
 namespace mgr {
+
+int device_sm_count()
+{
+    static std::atomic<int> cache[64];   // per device, 0 until read (zero-initialised: static storage)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+        cache[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
 
 struct Wt4 {
     double x, y, z, w;
@@ -208,20 +224,7 @@ void ck(cudaError_t e, const char *what)
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// SMs of the current device (cached per device)
-int num_sms()
-{
-    static int cache[64] = {0};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) return 152;
-    if (cache[dev] == 0) {
-        int n = 0;
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cache[dev] = n > 0 ? n : 1;
-    }
-    return cache[dev];
-}
+int num_sms() { return device_sm_count(); }
 
 // per-axis resampling plan of C1DScalar (downscale): gauss half width and
 // the 4 taps + weights of every output sample
