@@ -141,3 +141,31 @@ def test_batch_graphs_match_stream_launches_and_per_pair_driver():
         pp, csp, fp, npp = R.register_pair(mov, ref, 16.0, 2, mg, cost="ssd", penalty_weight=10.0)
         assert csg == csp
         assert abs(fg - fp) <= FINAL_COST_RTOL * abs(fp), (fg, fp)
+
+
+@pytest.mark.gpu
+def test_batch_of_identity_pairs_only():
+    """every pair holds one value per image: no level is made, nothing is
+    minimised, the parameters stay zero"""
+    from mia_gb300 import registration as R
+    pairs = [(np.full((40, 48), 2.0, np.float32), np.full((40, 48), 2.0, np.float32)),
+             (np.full((32, 32), -1.0, np.float32), np.full((32, 32), -1.0, np.float32))]
+    res = R.register_batch(pairs, 16.0, 2, R.minimizer("gsl", maxiter=5), cost="ssd", penalty_weight=10.0)
+    for pg, csg, fg, ng in res:
+        assert ng == 0 and fg == 0.0 and not np.any(pg)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batch_of_one_pair_equals_the_per_pair_driver(dim):
+    """one pair through the batch runs the per-pair driver's kernels in the
+    same order: the same final cost and parameters"""
+    from mia_gb300 import registration as R
+    mov, ref = _pair2d(81, (64, 72)) if dim == 2 else _pair3d(82, (24, 28, 32))
+    rate = 16.0 if dim == 2 else 8.0
+    mg = R.minimizer("gsl", maxiter=8, step=0.1)
+    (pb, cb, fb, nb), = R.register_batch([(mov, ref)], rate, 2, mg, cost="ssd", penalty_weight=10.0)
+    pp, cp, fp, npp = R.register_pair(mov, ref, rate, 2, mg, cost="ssd", penalty_weight=10.0)
+    assert cb == cp
+    assert abs(fb - fp) <= 1e-6 * abs(fp), (fb, fp)
+    assert np.linalg.norm(pb - pp) <= 1e-5 * max(np.linalg.norm(pp), 1e-12)
