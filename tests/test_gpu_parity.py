@@ -348,3 +348,29 @@ def test_levels_evaluated_concurrently_from_host_threads():
             assert rs[0] == rc[0] and rs[1] == rc[1]
             for a_, b_ in zip(rs[2:], rc[2:]):
                 np.testing.assert_array_equal(a_, b_)
+
+
+def test_large_volume_identity_and_constant_shift():
+    """size-independent properties at a large size (110 M voxels, extents
+    not multiples of the tiles): zero coefficients reproduce the moving
+    image (cost = the SSD of the two images); a constant coefficient field
+    shifts it by that amount (the cubic B-splines sum to one)"""
+    import mia_gb300 as M
+    size = (512, 480, 448)
+    z, y, x = np.meshgrid(*[np.arange(n, dtype=np.float32) for n in size[::-1]], indexing="ij", sparse=True)
+    src = (np.sin(x * 0.07) * np.cos(y * 0.05) + 0.5 * np.sin(z * 0.03 + 0.3 * x * 0.01)).astype(np.float32) * 100
+    ref = (src + 3.0 * np.cos(x * 0.011 + y * 0.013)).astype(np.float32)
+    lv = M.Level(size, rate=16.0, cost="ssd")
+    lv.set_images(src, ref)
+    p = np.zeros(lv.nparams)
+    ci, _ = lv.value(p)
+    expect = 0.5 * float(np.sum((src.astype(np.float64) - ref) ** 2))
+    assert abs(ci - expect) <= 1e-5 * expect, (ci, expect)
+    w = lv.warp(p)
+    assert float(np.max(np.abs(w - src))) <= 1e-4 * float(np.max(np.abs(src)))
+    p[0::3] = 2.0   # every coefficient's x component: u = (2, 0, 0)
+    w = lv.warp(p)
+    inner = (slice(2, -2), slice(2, -2), slice(4, -2))
+    shifted = np.roll(src, 2, axis=2)   # w(x) = src(x - 2)
+    assert float(np.max(np.abs(w[inner] - shifted[inner]))) <= 1e-3 * float(np.max(np.abs(src)))
+    lv.close()
