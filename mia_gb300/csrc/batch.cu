@@ -6,6 +6,7 @@
 // All pairs advance in lock step.  One step evaluates the cost+gradient of
 // every unfinished pair at the point its minimizer proposes:
 //   k_min_propose  (blocks x pairs) the minimizer's next evaluation point
+//                  (and, in 3D, its float copy that the warp kernel reads)
 //   warp, adjoint, gather of the split path over a work list of
 //                  (pair, tile) / (pair, block) items covering all pairs
 //   k_min_update   (blocks x pairs) the minimizer's decision
@@ -60,6 +61,7 @@ struct PairVec {
     double *x, *g, *xt, *gt;
     const double *costs;   // {image, penalty} at xt
     int n;
+    float *xf;             // 3D: the level's float copy of xt (written with xt), else null
 };
 
 // The minimizer kernels spread each pair's vectors over blocks of MCH
@@ -149,7 +151,11 @@ __global__ void __launch_bounds__(MT) k_min_propose(MinState *st, const PairVec 
         return;
     }
     if (s.phase == 0) {
-        for (int i = i0 + tid; i < i1; i += MT) v.xt[i] = v.x[i];
+        for (int i = i0 + tid; i < i1; i += MT) {
+            const double xi = v.x[i];
+            v.xt[i] = xi;
+            if (v.xf) v.xf[i] = float(xi);
+        }
         if (lead) active[p] = 1;
         return;
     }
@@ -167,6 +173,7 @@ __global__ void __launch_bounds__(MT) k_min_propose(MinState *st, const PairVec 
         for (int i = i0 + tid; i < i1; i += MT) {
             const double x1 = __dadd_rn(v.x[i], __dmul_rn(a, v.g[i]));
             v.xt[i] = x1;
+            if (v.xf) v.xf[i] = float(x1);
             if (x1 != v.x[i]) mv = 1;
         }
         mv = __syncthreads_or(mv);
@@ -195,7 +202,11 @@ __global__ void __launch_bounds__(MT) k_min_propose(MinState *st, const PairVec 
             return;
         }
         const double ms = -s.step;
-        for (int i = i0 + tid; i < i1; i += MT) v.xt[i] = __dadd_rn(v.xt[i], __dmul_rn(ms, v.g[i]));
+        for (int i = i0 + tid; i < i1; i += MT) {
+            const double xi = __dadd_rn(v.xt[i], __dmul_rn(ms, v.g[i]));
+            v.xt[i] = xi;
+            if (v.xf) v.xf[i] = float(xi);
+        }
         double d0 = 0.0, d1 = 0.0, d2 = 0.0;
         if (!pair_totals(m, p, nb, d0, d1, d2, red)) return;
         if (tid == 0) {
@@ -414,7 +425,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
         a.grad_penalty = nullptr;
         a.costs = r.costs.p;
         args[k] = a;
-        vecs[k] = PairVec{r.x.p, r.g.p, r.xt.p, r.gt.p, r.costs.p, int(n)};
+        vecs[k] = PairVec{r.x.p, r.g.p, r.xt.p, r.gt.p, r.costs.p, int(n), dim == 3 ? a.params_f : nullptr};
         MinState s{};
         s.step = mz.step;
         states[k] = s;
@@ -470,7 +481,6 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
 
     auto step = [&]() {
         k_min_propose<<<mgrid, MT, 0, st>>>(d_states, d_vecs, mz, d_active, msc);
-        if (dim == 3) launch_params_f32_batch(d_args, d_active, np, max_params, st);
         if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
                                 d_active, sm_warp, 0, st))
             throw std::invalid_argument("tile shape not compiled in");
@@ -485,7 +495,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     // kernel attributes are set outside the capture
     prepare_split_batch(dim, tile[0], tile[1], tile[2], sm_warp, sm_adj);
     cudaGraphExec_t exec = nullptr;
-    const unsigned kernels_per_chunk = unsigned(chunk) * (dim == 3 ? 6 : 5) + 1;
+    const unsigned kernels_per_chunk = unsigned(chunk) * 5 + 1;
     tr_setup.stop();
     if (use_graphs) {
         TraceScope tr("batch: graph capture", st);

@@ -99,8 +99,7 @@ void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int n
 // 3D split path (split3.cu): tiles of 32 x 8 x tz voxels, z-walking threads;
 // launch_warp3 converts the parameters to float first (launch_params_f32)
 void launch_params_f32(const EvalArgs &a, cudaStream_t st);
-// batch: every active pair's parameters (grid sized by the largest pair)
-void launch_params_f32_batch(const EvalArgs *args, const int *active, int npairs, size_t max_params, cudaStream_t st);
+// (the batched driver's minimizer writes the float copy with each trial point)
 bool tile_supported3(int tx, int ty, int tz);
 size_t split3_smem(const EvalArgs &a, int which);
 void launch_warp3(const EvalArgs &a, cudaStream_t st);

@@ -1053,27 +1053,9 @@ __global__ void __launch_bounds__(256) k_params_f32(const double *__restrict__ p
     for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) f[i] = float(p[i]);
 }
 
-// batch: grid (chunks, pairs); pairs whose minimizer has finished are skipped
-__global__ void __launch_bounds__(256) k_params_f32_batch(const EvalArgs *__restrict__ args,
-                                                          const int *__restrict__ active)
-{
-    if (!active[blockIdx.y]) return;
-    const EvalArgs &a = args[blockIdx.y];
-    const size_t n = size_t(a.nc[0]) * a.nc[1] * a.nc[2] * 3;
-    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256)
-        a.params_f[i] = float(a.params[i]);
-}
-
 // ---------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------
-void launch_params_f32_batch(const EvalArgs *args, const int *active, int npairs, size_t max_params, cudaStream_t st)
-{
-    const int chunks = int(std::min<size_t>(64, (max_params + 4095) / 4096));
-    k_params_f32_batch<<<dim3(std::max(chunks, 1), npairs), 256, 0, st>>>(args, active);
-    count_launch();
-}
-
 void launch_params_f32(const EvalArgs &a, cudaStream_t st)
 {
     const size_t n = size_t(a.nc[0]) * a.nc[1] * a.nc[2] * 3;
