@@ -374,3 +374,31 @@ def test_large_volume_identity_and_constant_shift():
     shifted = np.roll(src, 2, axis=2)   # w(x) = src(x - 2)
     assert float(np.max(np.abs(w[inner] - shifted[inner]))) <= 1e-3 * float(np.max(np.abs(src)))
     lv.close()
+
+
+@pytest.mark.parametrize("cost", ["ssd", "ncc"])
+def test_page_locked_host_buffers_give_the_same_results(cost):
+    """page-locked host buffers (the bench's end-to-end path) give the values
+    of pageable ones, and non-finite parameters are refused with either"""
+    import torch
+
+    import mia_gb300 as M
+    from mia_gb300 import _lib, synth
+    size = (40, 36, 28)
+    lv = M.Level(size, rate=5.0, cost=cost, penalty_weight=3.0)
+    a, b = make_pair(size[::-1], 12, ncc=cost == "ncc")
+    lv.set_images(a, b)
+    p = synth.smooth_params(lv.csize, 1.0, seed=13)
+    c1, g1 = lv.evaluate_total(p)
+    hp = torch.from_numpy(p.copy()).pin_memory().numpy()
+    hg = torch.empty(lv.nparams, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        c2, g2 = lv.evaluate_total(hp, hg)
+        assert c2 == c1
+        np.testing.assert_array_equal(hg, g1)
+    ci, cp, gi, gp, gt = lv.evaluate(hp)
+    np.testing.assert_array_equal(gt, g1)
+    hp[5] = np.nan
+    with pytest.raises(_lib.MgrError) as e:
+        lv.evaluate_total(hp, hg)
+    assert e.value.status == _lib.MGR_ERR_ARG
