@@ -536,7 +536,10 @@ mgr_status mgr_level_warp(mgr_level *lvl, const double *params, float *out)
         launch_warp(a, lvl->stream);
         check_launch("warp kernel");
         ck(cudaMemcpyAsync(out, lvl->warped.p, lvl->N * sizeof(float), cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        unsigned flag = 0;
+        read_status_flag(lvl, &flag);
         ck(cudaStreamSynchronize(lvl->stream), "warp sync");
+        throw_if_flagged(lvl, flag);
     });
 }
 
@@ -556,7 +559,10 @@ mgr_status mgr_level_force(mgr_level *lvl, const double *params, float *force, d
                            lvl->stream), "D2H");
         double sc[SC_NSLOTS];
         ck(cudaMemcpyAsync(sc, lvl->scalars.p, sizeof sc, cudaMemcpyDeviceToHost, lvl->stream), "D2H");
+        unsigned flag = 0;
+        read_status_flag(lvl, &flag);
         ck(cudaStreamSynchronize(lvl->stream), "force sync");
+        throw_if_flagged(lvl, flag);
         if (cost) *cost = sc[SC_FORCE_COST];
     });
 }

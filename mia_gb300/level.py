@@ -27,6 +27,14 @@ def _d(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _sized(a, n, what):
+    """`a` as given, after checking that it holds exactly n values (the C ABI
+    reads or writes n elements through the pointer)"""
+    if a.size != n:
+        raise ValueError(f"{what} must hold {n} values, got {a.size}")
+    return a
+
+
 class Level:
     """One image pair at one resolution level on one GPU.
 
@@ -86,6 +94,9 @@ class Level:
     def shape(self):
         return tuple(self.size[::-1])
 
+    def _params(self, params):
+        return _sized(_d(params), self.nparams, "params")
+
     def set_path(self, path="split", tile=(0, 0, 0)):
         p = _lib.PATH_PLAIN if path == "plain" else _lib.PATH_SPLIT
         t = list(tile) + [0] * (3 - len(tile))
@@ -100,7 +111,8 @@ class Level:
 
     def set_images(self, src, ref):
         s, r = _f(src), _f(ref)
-        assert s.shape == self.shape and r.shape == self.shape
+        if s.shape != self.shape or r.shape != self.shape:
+            raise ValueError(f"images must have shape {self.shape} ([z, y, x]), got {s.shape} and {r.shape}")
         check(lib().mgr_level_set_images(self.h, s.ctypes.data_as(_fp), r.ctypes.data_as(_fp)))
 
     def set_images_device(self, src_ptr, ref_ptr):
@@ -108,8 +120,7 @@ class Level:
 
     def evaluate(self, params):
         """(cost_image, cost_penalty, grad_image, grad_penalty, grad_total)"""
-        p = _d(params)
-        assert p.size == self.nparams
+        p = self._params(params)
         gt = np.empty(self.nparams)
         gi = np.empty(self.nparams)
         gp = np.empty(self.nparams)
@@ -121,8 +132,14 @@ class Level:
 
     def evaluate_total(self, params, grad_out=None):
         """cost+gradient as evaluate_fdf returns it (total cost, total gradient)."""
-        p = _d(params)
-        g = grad_out if grad_out is not None else np.empty(self.nparams)
+        p = self._params(params)
+        if grad_out is None:
+            g = np.empty(self.nparams)
+        else:
+            g = grad_out
+            if not (isinstance(g, np.ndarray) and g.dtype == np.float64 and g.flags.c_contiguous and g.flags.writeable):
+                raise ValueError("grad_out must be a writeable C-contiguous float64 array")
+            _sized(g, self.nparams, "grad_out")
         ci, cp = ctypes.c_double(), ctypes.c_double()
         check(lib().mgr_level_evaluate(self.h, p.ctypes.data_as(_dp), g.ctypes.data_as(_dp), None, None,
                                        ctypes.byref(ci), ctypes.byref(cp)))
@@ -133,26 +150,26 @@ class Level:
                                               ctypes.c_void_p(costs_ptr)))
 
     def value(self, params):
-        p = _d(params)
+        p = self._params(params)
         ci, cp = ctypes.c_double(), ctypes.c_double()
         check(lib().mgr_level_value(self.h, p.ctypes.data_as(_dp), ctypes.byref(ci), ctypes.byref(cp)))
         return ci.value, cp.value
 
     def warp(self, params):
-        p = _d(params)
+        p = self._params(params)
         out = np.empty(self.shape, np.float32)
         check(lib().mgr_level_warp(self.h, p.ctypes.data_as(_dp), out.ctypes.data_as(_fp)))
         return out
 
     def force(self, params):
-        p = _d(params)
+        p = self._params(params)
         out = np.empty(self.shape + (self.dim,), np.float32)
         c = ctypes.c_double()
         check(lib().mgr_level_force(self.h, p.ctypes.data_as(_dp), out.ctypes.data_as(_fp), ctypes.byref(c)))
         return c.value, out
 
     def translate(self, force):
-        f = _f(force)
+        f = _sized(_f(force), int(np.prod(self.shape)) * self.dim, "force")
         g = np.empty(self.nparams)
         check(lib().mgr_level_translate(self.h, f.ctypes.data_as(_fp), g.ctypes.data_as(_dp)))
         return g

@@ -37,8 +37,11 @@ def register_pair(src, ref, rate, levels, mz, path="split", device=0, **cost_kw)
     """Returns (params, csize, final_cost, evaluations)."""
     s = np.ascontiguousarray(src, dtype=np.float32)
     r = np.ascontiguousarray(ref, dtype=np.float32)
+    if s.shape != r.shape:
+        raise ValueError("source and reference differ in shape")
     d = level_desc(s.shape[::-1], rate, **cost_kw)
-    maxp = 1 << 24
+    # refine targets (size + rate - 1) / rate + 2 <= size + 2 coefficients per axis
+    maxp = int(np.prod([n + 3 for n in s.shape])) * s.ndim
     out = np.empty(maxp)
     cs = (ctypes.c_int * 3)()
     fc, ne = ctypes.c_double(), ctypes.c_int()
@@ -65,7 +68,11 @@ def refine_coefficients(params, nc_old, nc_new):
     """the spline grid refinement on the host: params (prod(nc_old) * dim,
     components interleaved, x fastest) onto nc_new; None when no axis grows"""
     dim = len(nc_old)
+    if len(nc_new) != dim:
+        raise ValueError("nc_old and nc_new differ in dimension")
     p = np.ascontiguousarray(params, dtype=np.float64)
+    if p.size != int(np.prod(nc_old)) * dim:
+        raise ValueError("params must hold prod(nc_old) * dim values")
     out = np.empty(int(np.prod(nc_new)) * dim)
     o = (ctypes.c_int * 3)(*(list(nc_old) + [1] * (3 - dim)))
     n = (ctypes.c_int * 3)(*(list(nc_new) + [1] * (3 - dim)))
@@ -143,6 +150,8 @@ def warp_image(img, csize, params, device=0):
 def normalize_pair(src, ref, device=0):
     s = np.ascontiguousarray(src, dtype=np.float32)
     r = np.ascontiguousarray(ref, dtype=np.float32)
+    if s.shape != r.shape:
+        raise ValueError("source and reference differ in shape")
     so, ro = np.empty_like(s), np.empty_like(r)
     m, sg, ok = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
     check(lib().mgr_normalize_pair(s.ctypes.data_as(_fp), r.ctypes.data_as(_fp), s.size, so.ctypes.data_as(_fp),

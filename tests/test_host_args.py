@@ -1,0 +1,25 @@
+"""Argument checks of the Python front end that run before any device call:
+buffers the C ABI would read past are refused with ValueError."""
+import numpy as np
+import pytest
+
+
+def test_pair_shapes_must_match():
+    from mia_gb300 import registration as R
+    a = np.zeros((8, 9, 10), np.float32)
+    b = np.zeros((8, 9, 11), np.float32)
+    mz = R.minimizer("gsl", maxiter=1, step=0.1)
+    with pytest.raises(ValueError):
+        R.register_pair(a, b, 4.0, 1, mz)
+    with pytest.raises(ValueError):
+        R.normalize_pair(a, b)
+    with pytest.raises(ValueError):
+        R.register_batch([(a, a), (a, b)], 4.0, 1, mz)
+
+
+def test_sized_helper():
+    from mia_gb300.level import _sized
+    a = np.zeros(12)
+    assert _sized(a, 12, "x") is a
+    with pytest.raises(ValueError, match="x must hold 13 values"):
+        _sized(a, 13, "x")

@@ -67,3 +67,12 @@ def test_device_refine_without_growth_writes_nothing():
     assert not R.refine_coefficients_device(d_in, d_out, (9, 9, 9), (9, 9, 9))
     torch.cuda.synchronize()
     assert torch.all(d_out == 7.0)
+
+
+def test_host_refine_rejects_wrong_sizes():
+    from mia_gb300 import registration as R
+    p = _params(3, (9, 9, 9), 3)
+    with pytest.raises(ValueError):
+        R.refine_coefficients(p[:-1], (9, 9, 9), (15, 15, 15))   # one value short of the old grid
+    with pytest.raises(ValueError):
+        R.refine_coefficients(p, (9, 9, 9), (15, 15))
