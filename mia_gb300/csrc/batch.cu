@@ -387,6 +387,7 @@ void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
     if (s == MGR_ERR_TIMEOUT) throw TimeoutError(mgr_last_error());
+    if (s == MGR_ERR_OOM) throw std::bad_alloc();
     if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
 }
 

@@ -25,6 +25,7 @@ void ckm(mgr_status s)
 {
     if (s == MGR_ERR_ARG) throw std::invalid_argument(mgr_last_error());
     if (s == MGR_ERR_TIMEOUT) throw TimeoutError(mgr_last_error());
+    if (s == MGR_ERR_OOM) throw std::bad_alloc();
     if (s != MGR_OK) throw std::runtime_error(mgr_last_error());
 }
 
@@ -196,6 +197,11 @@ extern "C" mgr_status mgr_scale_image(int dim, const int in_size[3], const float
         set_last_error("mgr_scale_image: invalid argument");
         return MGR_ERR_ARG;
     }
+    for (int k = 0; k < dim; ++k)
+        if (in_size[k] < 1 || out_size[k] < 1) {
+            set_last_error("mgr_scale_image: sizes must be positive");
+            return MGR_ERR_ARG;
+        }
     float *d_in = nullptr, *d_out = nullptr;
     cudaStream_t st = nullptr;
     try {

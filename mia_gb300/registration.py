@@ -148,6 +148,9 @@ def warp_image(img, csize, params, device=0):
 
 
 def normalize_pair(src, ref, device=0):
+    """(applied, src', ref', mean, sigma): the joint mean-0 / sigma-1
+    normalisation; when both images hold one value nothing is applied and
+    src', ref' are copies of the inputs"""
     s = np.ascontiguousarray(src, dtype=np.float32)
     r = np.ascontiguousarray(ref, dtype=np.float32)
     if s.shape != r.shape:
@@ -157,7 +160,9 @@ def normalize_pair(src, ref, device=0):
     check(lib().mgr_normalize_pair(s.ctypes.data_as(_fp), r.ctypes.data_as(_fp), s.size, so.ctypes.data_as(_fp),
                                    ro.ctypes.data_as(_fp), ctypes.byref(m), ctypes.byref(sg), ctypes.byref(ok),
                                    int(device)))
-    return bool(ok.value), so, ro, m.value, sg.value
+    if not ok.value:
+        return False, s.copy(), r.copy(), m.value, sg.value
+    return True, so, ro, m.value, sg.value
 
 
 def _batch(shapes, sptrs, rptrs, on_device, rate, levels, mz, device, use_graphs, cost_kw):

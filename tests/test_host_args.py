@@ -23,3 +23,14 @@ def test_sized_helper():
     assert _sized(a, 12, "x") is a
     with pytest.raises(ValueError, match="x must hold 13 values"):
         _sized(a, 13, "x")
+
+
+def test_scale_image_rejects_non_positive_sizes():
+    import ctypes
+    from mia_gb300 import _lib
+    a = np.zeros(16, np.float32)
+    fp = a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    isz = (ctypes.c_int * 3)(4, 4, 1)
+    osz = (ctypes.c_int * 3)(2, 0, 1)
+    assert _lib.lib().mgr_scale_image(2, isz, fp, osz, fp, 0) == _lib.MGR_ERR_ARG
+    assert b"positive" in _lib.lib().mgr_last_error()
