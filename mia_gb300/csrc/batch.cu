@@ -614,8 +614,10 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             if (d.dim != dim) throw std::invalid_argument("all pairs of a batch must have the same dimension");
             if (d.cost != descs[0].cost || d.has_penalty != descs[0].has_penalty)
                 throw std::invalid_argument("all pairs of a batch must use the same cost and penalty");
-            for (int k = 0; k < dim; ++k)
+            for (int k = 0; k < dim; ++k) {
                 if (d.csize[k] != 0) throw std::invalid_argument("the batch derives the grids from the rate");
+                if (d.size[k] < 2) throw std::invalid_argument("image dimensions must be >= 2");
+            }
         }
         if (mz->kind != MGR_MIN_GSL_SD && mz->kind != MGR_MIN_GDSQ) throw std::invalid_argument("unknown minimizer");
         ck(cudaSetDevice(device), "cudaSetDevice");

@@ -139,8 +139,10 @@ extern "C" mgr_status mgr_register(const mgr_level_desc *desc, int levels, const
     try {
         if (levels < 1) throw std::invalid_argument("levels must be >= 1");
         if (desc->dim != 2 && desc->dim != 3) throw std::invalid_argument("dim must be 2 or 3");
-        for (int k = 0; k < desc->dim; ++k)
+        for (int k = 0; k < desc->dim; ++k) {
             if (desc->csize[k] != 0) throw std::invalid_argument("mgr_register derives the grid from the rate");
+            if (desc->size[k] < 2) throw std::invalid_argument("image dimensions must be >= 2");
+        }
         if (mz->kind != MGR_MIN_GSL_SD && mz->kind != MGR_MIN_GDSQ) throw std::invalid_argument("unknown minimizer");
         if (mz->maxiter < 1) throw std::invalid_argument("maxiter must be >= 1");
         ck(cudaSetDevice(device), "cudaSetDevice");

@@ -34,3 +34,20 @@ def test_scale_image_rejects_non_positive_sizes():
     osz = (ctypes.c_int * 3)(2, 0, 1)
     assert _lib.lib().mgr_scale_image(2, isz, fp, osz, fp, 0) == _lib.MGR_ERR_ARG
     assert b"positive" in _lib.lib().mgr_last_error()
+
+
+def test_registration_rejects_degenerate_sizes():
+    """sizes below 2 are refused before any device call"""
+    import ctypes
+    from mia_gb300 import _lib
+    from mia_gb300 import registration as R
+    a = np.zeros(4, np.float32)
+    fp = a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    mz = R.minimizer("gsl", maxiter=1)
+    d = R.level_desc((4, 1), 2.0)
+    out = np.empty(64)
+    cs = (ctypes.c_int * 3)()
+    st = _lib.lib().mgr_register(ctypes.byref(d), 1, ctypes.byref(mz), fp, fp, _lib.PATH_SPLIT, 0,
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size, cs, None, None)
+    assert st == _lib.MGR_ERR_ARG
+    assert b">= 2" in _lib.lib().mgr_last_error()
