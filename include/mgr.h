@@ -76,7 +76,9 @@ const char *mgr_last_error(void);
    (mia/3d/transform/spline.cc:102-147, 224-275), the divcurl penalty
    initialize (mia/3d/splinetransformpenalty.cc:43-49) and the image full
    cost set_size (mia/3d/fullcost/image.cc:80-98).  `stream` is a
-   cudaStream_t or NULL for a stream owned by the level. */
+   cudaStream_t or NULL for a stream owned by the level.  A caller's stream
+   must outlive the level: the level's device buffers are allocated and
+   freed in its order. */
 mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream,
                             mgr_level **out);
 /* Releases the level.  Its device buffers are freed in stream order: on a
@@ -107,7 +109,10 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
                               double *cost_image, double *cost_penalty);
 
 /* Device variant: params / grad_total are device pointers (nparams doubles),
-   d_costs receives {cost_image, cost_penalty} (2 doubles, device). */
+   d_costs receives {cost_image, cost_penalty} (2 doubles, device).  The
+   kernels are only queued on the level's stream (no synchronisation, no
+   finite check of the parameters); a bounded device wait that gave up is
+   reported by the next mgr_level_sync. */
 mgr_status mgr_level_evaluate_device(mgr_level *lvl, const double *d_params,
                                      double *d_grad_total, double *d_costs);
 
@@ -285,7 +290,8 @@ mgr_status mgr_transform_load(const char *path, int *dim, int size[3], int csize
                               size_t creator_cap, char *attrs, size_t attrs_cap, double *params,
                               size_t params_cap, size_t *nparams);
 
-/* Wait for all work queued on the level's stream. */
+/* Wait for all work queued on the level's stream; MGR_ERR_TIMEOUT when a
+   bounded device wait of that work gave up (the flag is then cleared). */
 mgr_status mgr_level_sync(mgr_level *lvl);
 
 /* Number of kernels this library has launched in the calling process
