@@ -51,3 +51,21 @@ def test_registration_rejects_degenerate_sizes():
                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size, cs, None, None)
     assert st == _lib.MGR_ERR_ARG
     assert b">= 2" in _lib.lib().mgr_last_error()
+
+
+def test_level_methods_refuse_wrong_sizes_before_the_device_call():
+    """a Level without a device handle: each method raises ValueError on a
+    wrong-size buffer before it would reach the C ABI"""
+    from mia_gb300.level import Level
+    lv = Level.__new__(Level)
+    lv.h, lv.dim, lv.size, lv.nparams = None, 3, (5, 4, 3), 24
+    short = np.zeros(23)
+    for call in (lambda: lv.evaluate(short), lambda: lv.evaluate_total(short), lambda: lv.value(short),
+                 lambda: lv.warp(short), lambda: lv.force(short),
+                 lambda: lv.evaluate_total(np.zeros(24), grad_out=np.zeros(23)),
+                 lambda: lv.evaluate_total(np.zeros(24), grad_out=np.zeros(24, np.float32)),
+                 lambda: lv.evaluate_total(np.zeros(24), grad_out=np.zeros(48)[::2]),
+                 lambda: lv.translate(np.zeros((3, 4, 5, 2), np.float32)),
+                 lambda: lv.set_images(np.zeros((3, 4, 5)), np.zeros((3, 4, 6)))):
+        with pytest.raises(ValueError):
+            call()
