@@ -283,9 +283,10 @@ mgr_status mgr_transform_save(const char *path, int dim, const int size[3], cons
 
 /* Reads what mgr_transform_save wrote.  Writes dim, size, csize,
    *nparams; the creator string and the attributes ("name\tvalue\n" lines,
-   csize excluded) when their buffers are given; the parameters when
-   `params` is given (params_cap >= *nparams).  Call with params = NULL to
-   learn *nparams first. */
+   csize excluded) when their buffers are given (MGR_ERR_ARG, naming the
+   size needed, when a string does not fit with its terminating zero); the
+   parameters when `params` is given (params_cap >= *nparams).  Call with
+   params = NULL to learn *nparams first. */
 mgr_status mgr_transform_load(const char *path, int *dim, int size[3], int csize[3], char *creator,
                               size_t creator_cap, char *attrs, size_t attrs_cap, double *params,
                               size_t params_cap, size_t *nparams);

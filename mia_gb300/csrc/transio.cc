@@ -267,16 +267,22 @@ extern "C" mgr_status mgr_transform_load(const char *path, int *dim, int size[3]
         if (nc != t.params.size()) throw std::invalid_argument("archive: params do not match csize");
         for (int k = 0; k < 3; ++k) csize[k] = c[k];
         *nparams = t.params.size();
+        // strings are copied whole or not at all: a buffer too small is an
+        // error that names the size needed
         if (creator && creator_cap) {
-            std::strncpy(creator, t.creator.c_str(), creator_cap - 1);
-            creator[creator_cap - 1] = '\0';
+            if (t.creator.size() + 1 > creator_cap)
+                throw std::invalid_argument("creator buffer too small: " + std::to_string(t.creator.size() + 1) +
+                                            " bytes needed");
+            std::memcpy(creator, t.creator.c_str(), t.creator.size() + 1);
         }
         if (attrs && attrs_cap) {   // "name\tvalue\n" per attribute other than csize
             std::string a;
             for (auto &kv : t.attr)
                 if (kv.first != "csize") a += kv.first + "\t" + kv.second + "\n";
-            std::strncpy(attrs, a.c_str(), attrs_cap - 1);
-            attrs[attrs_cap - 1] = '\0';
+            if (a.size() + 1 > attrs_cap)
+                throw std::invalid_argument("attribute buffer too small: " + std::to_string(a.size() + 1) +
+                                            " bytes needed");
+            std::memcpy(attrs, a.c_str(), a.size() + 1);
         }
         if (params) {
             if (params_cap < t.params.size()) throw std::invalid_argument("params buffer too small");

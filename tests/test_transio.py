@@ -58,3 +58,21 @@ def test_save_rejects_a_parameter_count_that_does_not_match_the_grid(tmp_path):
         R.save_transform(tmp_path / "t.x3dt", (20, 22, 23), (4, 4, 4), np.zeros(10))
     assert e.value.status == _lib.MGR_ERR_ARG
     assert not os.path.exists(tmp_path / "t.x3dt")
+
+
+def test_load_refuses_string_buffers_too_small(tmp_path):
+    """strings are returned whole: a buffer too small is an error naming the size needed"""
+    import ctypes
+    from mia_gb300 import _lib
+    from mia_gb300 import registration as R
+    f = tmp_path / "t.x2dt"
+    R.save_transform(f, (20, 18), (5, 5), np.zeros(50), rate=6, attributes={"a": "x" * 40})
+    dim, n = ctypes.c_int(), ctypes.c_size_t()
+    sz, cs = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    small = ctypes.create_string_buffer(8)
+    st = _lib.lib().mgr_transform_load(str(f).encode(), ctypes.byref(dim), sz, cs, small, len(small), None, 0,
+                                       None, 0, ctypes.byref(n))
+    assert st == _lib.MGR_ERR_ARG and b"14 bytes needed" in _lib.lib().mgr_last_error()
+    st = _lib.lib().mgr_transform_load(str(f).encode(), ctypes.byref(dim), sz, cs, None, 0, small, len(small),
+                                       None, 0, ctypes.byref(n))
+    assert st == _lib.MGR_ERR_ARG and b"44 bytes needed" in _lib.lib().mgr_last_error()
