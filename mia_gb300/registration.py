@@ -6,6 +6,7 @@ built with the `scale` filter, upscale and refine of the spline
 transformation, the `gsl:opt=gd` or `gdsq` minimizer per level.
 """
 import ctypes
+import re
 
 import numpy as np
 
@@ -123,10 +124,19 @@ def load_transform(path):
     check(lib().mgr_transform_load(str(path).encode(), ctypes.byref(dim), sz, cs, None, 0, None, 0, None, 0,
                                    ctypes.byref(n)))
     params = np.empty(n.value)
-    creator = ctypes.create_string_buffer(4096)
-    attrs = ctypes.create_string_buffer(1 << 16)
-    check(lib().mgr_transform_load(str(path).encode(), ctypes.byref(dim), sz, cs, creator, len(creator), attrs,
-                                   len(attrs), params.ctypes.data_as(_dp), params.size, ctypes.byref(n)))
+    cap = {"creator": 4096, "attribute": 1 << 16}
+    for _ in range(3):   # a string too large for its buffer: grow it to the size the error names
+        creator = ctypes.create_string_buffer(cap["creator"])
+        attrs = ctypes.create_string_buffer(cap["attribute"])
+        status = lib().mgr_transform_load(str(path).encode(), ctypes.byref(dim), sz, cs, creator, len(creator),
+                                          attrs, len(attrs), params.ctypes.data_as(_dp), params.size,
+                                          ctypes.byref(n))
+        m = re.match(r".*(creator|attribute) buffer too small: (\d+) bytes needed",
+                     lib().mgr_last_error().decode()) if status == _lib.MGR_ERR_ARG else None
+        if not m:
+            break
+        cap[m.group(1)] = int(m.group(2))
+    check(status)
     d = dim.value
     attributes = dict(line.split("\t", 1) for line in attrs.value.decode().splitlines() if line)
     return dict(dim=d, size=tuple(sz[:d]), csize=tuple(cs[:d]), creator=creator.value.decode(),

@@ -76,3 +76,13 @@ def test_load_refuses_string_buffers_too_small(tmp_path):
     st = _lib.lib().mgr_transform_load(str(f).encode(), ctypes.byref(dim), sz, cs, None, 0, small, len(small),
                                        None, 0, ctypes.byref(n))
     assert st == _lib.MGR_ERR_ARG and b"44 bytes needed" in _lib.lib().mgr_last_error()
+
+
+def test_load_returns_large_attribute_maps(tmp_path):
+    from mia_gb300 import registration as R
+    f = tmp_path / "t.x3dt"
+    attrs = {"k%03d" % i: "v" * 1000 for i in range(100)}   # about 100 KB of attributes
+    R.save_transform(f, (20, 18, 16), (5, 5, 5), np.ones(375), creator="spline:rate=" + "9" * 5000,
+                     attributes=attrs)
+    t = R.load_transform(f)
+    assert t["attributes"] == attrs and t["creator"] == "spline:rate=" + "9" * 5000
