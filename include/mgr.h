@@ -205,7 +205,10 @@ typedef struct {
    the host and evaluates through mgr_level_evaluate (one device round trip
    per evaluation: the plain per-pair drop-in).  Writes the final
    coefficient grid, its parameters (max_params doubles), the cost at the
-   returned parameters and the number of cost+gradient evaluations. */
+   returned parameters and the number of cost+gradient evaluations.  The
+   grid has at most size + 2 coefficients per axis (rate >= 1), so
+   prod(size[k] + 2) * dim doubles always suffice; a smaller buffer that
+   cannot hold the result is MGR_ERR_ARG after the run. */
 mgr_status mgr_register(const mgr_level_desc *desc, int levels, const mgr_minimizer_desc *mz,
                         const float *src, const float *ref, int path, int device,
                         double *params_out, size_t max_params, int csize_out[3],
@@ -221,7 +224,7 @@ mgr_status mgr_register(const mgr_level_desc *desc, int levels, const mgr_minimi
    pair with one launch per kernel over a (pair, tile) work list; with
    `use_graphs` the steps of each level are captured as a CUDA graph.
    csize_out holds 3 ints per pair; params_out[p] receives max_params[p]
-   doubles at most. */
+   doubles at most (sized as for mgr_register). */
 mgr_status mgr_register_batch(int npairs, const mgr_level_desc *descs, int levels,
                               const mgr_minimizer_desc *mz, const float *const *srcs,
                               const float *const *refs, int device, int use_graphs,
