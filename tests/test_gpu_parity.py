@@ -179,6 +179,42 @@ def test_edge_sizes(size, rate):
     check_eval(g, o, o64, synth.smooth_params(g.csize, 0.8, seed=2))
 
 
+@pytest.mark.parametrize("size,rate", [((5, 4), 1.0), ((130, 9), 2.0), ((33, 31), 16.0)])
+def test_edge_sizes_2d(size, rate):
+    g, o, o64 = both(size, rate=rate, cost="ssd", penalty_weight=1.0)
+    mov, ref = make_pair(size[::-1], 19)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 0.8, seed=4))
+
+
+@pytest.mark.parametrize("cost", ["ssd", "ncc"])
+@pytest.mark.parametrize("size,rate", [((33, 27, 19), (3.0, 5.0, 7.0)), ((57, 43), (4.0, 9.0))])
+def test_anisotropic_rate_with_cost_and_penalty_options(size, rate, cost):
+    """a different spline rate per axis, with the image cost's weight and
+    norm and the divcurl penalty's div, curl and norm away from their defaults"""
+    g, o, o64 = both(size, rate=rate, cost=cost, ssd_norm=cost == "ssd", cost_weight=0.6, penalty_weight=4.0,
+                     div=2.0, curl=0.3, penalty_norm=True)
+    mov, ref = make_pair(size[::-1], 23, ncc=cost == "ncc")
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 1.2, seed=6))
+
+
+@pytest.mark.parametrize("size,csize", [((30, 26, 22), (9, 6, 7)), ((44, 38), (5, 11))])
+def test_explicit_coefficient_grid(size, csize):
+    """a coefficient grid given directly (as after refine), not derived from a rate"""
+    g, o, o64 = both(size, csize=csize, cost="ncc", penalty_weight=2.0)
+    assert g.csize == tuple(csize)
+    mov, ref = make_pair(size[::-1], 29, ncc=True)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 1.0, seed=8))
+
+
 def test_tiles_and_determinism():
     size = (70, 41, 23)
     g, o, o64 = both(size, rate=5.0, cost="ncc", penalty_weight=2.0)
