@@ -193,3 +193,25 @@ def test_batch_from_device_images_equals_host_images_and_matches_oracle():
     for (mov, ref), (pg, csg, fg, ng) in zip(pairs, host):
         po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, 8.0, 3, mo, **kw)
         _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batch_ncc_without_penalty_matches_oracle(dim):
+    """NCC with no spline penalty (the image term alone), GSL steepest descent"""
+    from mia_gb300 import registration as R
+    from mia_gb300 import synth
+    if dim == 2:
+        shapes, rate = [(72, 88), (96, 80)], 16.0
+        pairs = [_pair2d(101 + 3 * i, s, rate) for i, s in enumerate(shapes)]
+        pairs = [((m * synth.bias_field(m.shape, 0.1, seed=7 + i)).astype(np.float32), r)
+                 for i, (m, r) in enumerate(pairs)]
+    else:
+        shapes, rate = [(40, 36, 44), (36, 44, 40)], 8.0
+        pairs = [_pair3d(111 + 3 * i, s, rate) for i, s in enumerate(shapes)]
+    mg = R.minimizer("gsl", maxiter=8, step=0.1)
+    res = R.register_batch(pairs, rate, 2, mg, cost="ncc")
+    mo = O.minimizer("gsl", maxiter=8, step=0.1)
+    for (mov, ref), (pg, csg, fg, ng) in zip(pairs, res):
+        po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, rate, 2, mo, cost="ncc")
+        _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
