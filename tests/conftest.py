@@ -12,6 +12,15 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def pytest_sessionstart(session):
+    # libmgr.so is built in-tree when it is missing (nvcc cross-compiles for
+    # sm_103a without a GPU), as the oracle's library is on first use
+    from mia_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from mia_gb300 import build
+        build.build()
+
+
 @pytest.fixture(scope="session")
 def goldens():
     import json
