@@ -298,6 +298,14 @@ mgr_status mgr_transform_load(const char *path, int *dim, int size[3], int csize
    bounded device wait of that work gave up (the flag is then cleared). */
 mgr_status mgr_level_sync(mgr_level *lvl);
 
+/* Self-test of the bounded device waits (no counterpart in the reference):
+   one thread waits on a barrier that nothing completes, with the warp
+   kernel's wait at a limit of 1024 tries.  *gave_up = 1 when the wait ended
+   by its limit and raised its flag (the expected result); *us_per_try is
+   the time of one failed try, from which the production limit (2^20 tries)
+   takes its duration.  The device stays usable afterwards. */
+mgr_status mgr_selftest_bounded_wait(int device, int *gave_up, double *us_per_try);
+
 /* Number of kernels this library has launched in the calling process
    (for launch accounting in benchmarks). */
 unsigned long long mgr_kernel_launch_count(void);

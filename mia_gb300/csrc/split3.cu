@@ -37,10 +37,14 @@
 //       (mia/3d/splinetransformpenalty.cc:60-71) and the full-cost weight
 //       (mia/template/fullcost.cxx:37-45).
 #include <algorithm>
+#include <string>
 
+#include "../../include/mgr.h"
 #include "mgr_cost.cuh"
 
 namespace mgr {
+
+void set_last_error(const std::string &msg);
 
 namespace {
 
@@ -107,11 +111,12 @@ __device__ __forceinline__ unsigned smem_u32(const void *p)
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
-// Bounded wait on phase `parity` of an mbarrier: false after the iteration
-// limit (the copy engine did not deliver), so that no wait is endless.
+// Bounded wait on phase `parity` of an mbarrier: false after LIMIT tries
+// (the copy engine did not deliver), so that no wait is endless.
+template <int LIMIT = (1 << 20)>
 __device__ __forceinline__ bool mbar_wait(unsigned mb, unsigned parity)
 {
-    for (int it = 0; it < (1 << 20); ++it) {
+    for (int it = 0; it < LIMIT; ++it) {
         unsigned done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                      : "=r"(done)
@@ -1178,3 +1183,56 @@ void launch_gather3_batch(const EvalArgs *args, const int2 *items, int nitems, c
 }
 
 }  // namespace mgr
+
+// Self-test of the bounded wait: one thread waits on phase 0 of an mbarrier
+// that nothing arrives at (no copy is in flight), with the warp kernel's
+// wait at a limit of SELFTEST_TRIES tries; it must give up and raise the
+// flag, and the clock cycles it spent give the time of one failed try.
+namespace {
+constexpr int SELFTEST_TRIES = 1024;
+
+__global__ void k_bounded_wait_selftest(unsigned *flag, long long *cycles)
+{
+    __shared__ __align__(8) unsigned long long mb;
+    const unsigned a = mgr::smem_u32(&mb);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    const long long t0 = clock64();
+    if (!mgr::mbar_wait<SELFTEST_TRIES>(a, 0u)) atomicOr(flag, 1u);
+    *cycles = clock64() - t0;
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(a) : "memory");
+}
+}  // namespace
+
+extern "C" mgr_status mgr_selftest_bounded_wait(int device, int *gave_up, double *us_per_try)
+{
+    if (!gave_up || !us_per_try) {
+        mgr::set_last_error("mgr_selftest_bounded_wait: null argument");
+        return MGR_ERR_ARG;
+    }
+    unsigned *flag = nullptr;
+    long long *cycles = nullptr;
+    unsigned f = 0;
+    long long c = 0;
+    int khz = 0;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMalloc(&flag, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&cycles, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMemset(flag, 0, sizeof(unsigned));
+    if (e == cudaSuccess) {
+        k_bounded_wait_selftest<<<1, 1>>>(flag, cycles);
+        mgr::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&f, flag, sizeof f, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&c, cycles, sizeof c, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device);
+    cudaFree(flag);
+    cudaFree(cycles);
+    if (e != cudaSuccess) {
+        mgr::set_last_error(std::string("mgr_selftest_bounded_wait: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? MGR_ERR_OOM : MGR_ERR_CUDA;
+    }
+    *gave_up = f ? 1 : 0;
+    *us_per_try = khz > 0 ? double(c) / (double(khz) * 1e-3) / SELFTEST_TRIES : 0.0;
+    return MGR_OK;
+}

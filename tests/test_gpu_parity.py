@@ -438,3 +438,24 @@ def test_page_locked_host_buffers_give_the_same_results(cost):
     with pytest.raises(_lib.MgrError) as e:
         lv.evaluate_total(hp, hg)
     assert e.value.status == _lib.MGR_ERR_ARG
+
+
+def test_bounded_wait_gives_up_and_the_device_stays_usable():
+    """a wait on a barrier that nothing completes ends by its limit and
+    raises the flag (no fault, no hang); an evaluation afterwards still
+    matches the oracle"""
+    import ctypes
+    from mia_gb300 import _lib
+    gave_up, us = ctypes.c_int(-1), ctypes.c_double(-1.0)
+    _lib.check(_lib.lib().mgr_selftest_bounded_wait(0, ctypes.byref(gave_up), ctypes.byref(us)))
+    assert gave_up.value == 1
+    assert us.value > 0.0
+    print("one failed try of the bounded wait: %.4g us (production limit 2^20 tries: %.3g s)"
+          % (us.value, us.value * 2 ** 20 * 1e-6))
+    size = (24, 20, 18)
+    g, o, o64 = both(size, rate=4.0, cost="ssd", penalty_weight=1.0)
+    mov, ref = make_pair(size[::-1], 13)
+    for lv in (g, o, o64):
+        lv.set_images(mov, ref)
+    from mia_gb300 import synth
+    check_eval(g, o, o64, synth.smooth_params(g.csize, 1.0, seed=5))
