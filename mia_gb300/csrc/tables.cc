@@ -12,7 +12,6 @@
 #include <cstdint>
 #include <cstring>
 #include <deque>
-#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -44,51 +43,20 @@ void weights3(double x, double w[4])
     w[2] = ((x - w3) - w3) + w0;
 }
 
-// bspline<3,k>::apply (bspline.cc:328-375)
-double bspline3(double x, int deg)
+// Value of the cubic B-spline at x (bspline<3,0>::apply,
+// mia/core/splinekernel/bspline.cc:328-345): the transposed rows of
+// build_axis carry these values rounded to float, so the expression and
+// its rounding are kept.
+double bspline3_value(double x)
 {
-    if (deg == 0) {
-        x = std::fabs(x);
-        if (x <= 1.0) return 2.0 / 3.0 - x * x * (1 - 0.5 * x);
-        if (x < 2.0) {
-            const double dx = 2.0 - x;
-            return dx * dx * dx * (1.0 / 6.0);
-        }
-        return 0.0;
-    }
-    if (deg == 1) {
-        const double ax = std::fabs(x);
-        if (ax <= 1.0) return (1.5 * ax - 2) * x;
-        if (ax <= 2.0) return (x > 0.0 ? -0.5 : 0.5) * (2 - ax) * (2 - ax);
-        return 0.0;
-    }
     x = std::fabs(x);
-    if (x > 2.0) return 0.0;
-    if (x > 1.0) return 2.0 - x;
-    return 3.0 * x - 2.0;
+    if (x <= 1.0) return 2.0 / 3.0 - x * x * (1 - 0.5 * x);
+    if (x < 2.0) {
+        const double dx = 2.0 - x;
+        return dx * dx * dx * (1.0 / 6.0);
+    }
+    return 0.0;
 }
-
-// integrate2 + simpson for the cubic kernel (mia/core/splinekernel.cc:287-315,
-// mia/core/simpson.hh:36-51)
-double integrate2(double s1, double s2, int d1, int d2, double x0, double L)
-{
-    double a = s1 - 2.0, b = s1 + 2.0;
-    if (a < s2 - 2.0) a = s2 - 2.0;
-    if (a < x0) a = x0;
-    if (b > s2 + 2.0) b = s2 + 2.0;
-    if (b > L) b = L;
-    if (b <= a) return 0.0;
-    const size_t intervals = size_t(8 * (b - a));
-    auto f = [&](double x) { return bspline3(x - s1, d1) * bspline3(x - s2, d2); };
-    const double dx = (b - a) / intervals;
-    double sum = 0.5 * (f(a) + f(b));
-    double x = a + dx;
-    for (size_t i = 1; i < intervals; ++i, x += dx) sum += f(x);
-    x = a + .5 * dx;
-    for (size_t i = 0; i < intervals; ++i, x += dx) sum += 2 * f(x);
-    return sum * dx / 3.0;
-}
-
 }  // namespace
 
 int csize_from_rate(int size, float rate)
@@ -135,7 +103,7 @@ void build_axis(AxisHost &ax, int n, int nc, int tile)
             const double x = double(i) * double(scale) + 1.0 - double(o);
             if (std::fabs(x) < 2.0) {
                 if (first < 0) first = i;
-                const double y = bspline3(x, 0);
+                const double y = bspline3_value(x);
                 if (y > 0) {
                     ++len;
                     per_voxel[i].push_back({o, float(y)});
@@ -189,146 +157,272 @@ void build_axis(AxisHost &ax, int n, int nc, int tile)
     }
 }
 
-// C3DPPDivcurlMatrixImpl::reset (mia/3d/ppmatrix.cc:175-290), including
-// CIntegralCache2's first-lookup-returns-0 behaviour (ppmatrix.cc:147-165).
-std::vector<float> build_penalty3(const int csize[3], const float range[3], double wdiv, double wrot)
+// ---------------------------------------------------------------------
+// divcurl penalty
+// ---------------------------------------------------------------------
+// The `divcurl` spline penalty (mia/3d/ppmatrix.cc, mia/2d/ppmatrix.cc)
+// of a spline field u = sum_i c_i B(x - i) (B the cubic B-spline per axis,
+// coordinates in coefficient units) is the energy
+//
+//   E(u) = int wdiv |grad(div u)|^2 + wrot |grad(curl u)|^2 dx,
+//
+// a quadratic form in the coefficients with one d x d block per pair of
+// coefficients (i, j).  Every second derivative of u is a sum of
+// coefficients times products of per-axis B-spline derivatives, so every
+// entry of a block is a sum of terms
+//
+//   w * prod_axes J_a(alpha_a, beta_a; i_a, j_a),
+//   J(p, q; s, t) = h^(p+q) int B^(p)(x - s) B^(q)(x - t) dx,
+//
+// where alpha and beta are the derivative orders taken at i and at j (two
+// per term: each term pairs one second derivative at i with one at j) and
+// h = (n_c - 1) / range converts coefficient units to image units.  The
+// builders tabulate J per axis and derivative pair and assemble the blocks
+// from a term list that follows from the two operators:
+//
+//   grad(div u):  for every axis a the form sum_c d_a d_c u_c, so block
+//                 (c, c') gets wdiv * K(a + c, a + c') summed over a;
+//   grad(curl u): |curl v|^2 = |grad v|^2 - tr(grad v grad v) for
+//                 v = d_a u, so block (c, c) gets wrot * K(a + b, a + b)
+//                 for every axis a and every b != c, and the pair of
+//                 blocks (c, c'), (c', c) gets -2 wrot K(a + c', a + c);
+//
+// with K(alpha, beta) the product of the J over the axes.  Conventions of
+// the reference that these tables follow (they decide values, not only
+// rounding):
+//
+//   R1  quadrature: J is the composite Simpson sum on 8 panels per unit
+//       interval of the supports' overlap (the reference integrates with
+//       mia/core/splinekernel.cc:287-315 and mia/core/simpson.hh:36-51);
+//       for these piecewise polynomials that is not the exact integral;
+//   R2  powers of h are float products h, h*h, h*(h*h), ... and the global
+//       factor is 1 / (h_x h_y [h_z]) of the float product
+//       (mia/3d/ppmatrix.cc:191-197, mia/2d/ppmatrix.cc:195-199);
+//   R3  cross entries store both orderings of the pair in one number and
+//       write the curl part in the derivative order of the div part,
+//       2 (wdiv - wrot) sum_a K(a + c, a + c'): the two orders agree by
+//       integration by parts when the integrals cover the whole overlap;
+//       the reference uses this form also for the boundary-clipped 2D
+//       integrals, where they do not;
+//   R4  in the (x, y) entry the term of the last axis is taken in the
+//       opposite order, K(a + y, a + x) (mia/3d/ppmatrix.cc:269-272,
+//       mia/2d/ppmatrix.cc:230); with whole-overlap 3D integrals the two
+//       orders agree to rounding, with the clipped 2D ones they do not;
+//   R5  3D integrals run over the whole overlap for every pair (no image
+//       boundary), so one 9^3 table of offsets d = i - j serves the grid;
+//       2D integrals are clipped to [0, n_c] on each axis, so 2D blocks
+//       depend on the position and are listed per pair (i, j), the rows of
+//       i in order of j;
+//   R6  offsets of 4 or more coefficients have disjoint supports and are
+//       zero (the reference's 3D table keeps them, its 2D list drops every
+//       pair whose three values are all zero, mia/2d/ppmatrix.cc:237).
+namespace {
+
+// B^(p)(x) of the cubic B-spline, p = 0, 1, 2, from its polynomial pieces
+// in t = |x|: (4 - 6 t^2 + 3 t^3) / 6 on [0, 1] and (2 - t)^3 / 6 on [1, 2]
+double cubic_bspline_derivative(double x, int p)
 {
-    struct Cache {
-        int d1, d2;
-        bool valid[9] = {false};
-        double val[9] = {0};
-        double get(int delta)
-        {
-            delta += 4;
-            if (delta < 0 || delta >= 9) return 0;
-            double r = 0;
-            if (valid[delta]) r = val[delta];
-            else {
-                val[delta] = integrate2(4, delta, d1, d2, 0, 8);
-                valid[delta] = true;
-            }
-            return r;
-        }
-    };
-    Cache rc00{0, 0}, rc11{1, 1}, rc22{2, 2}, rc21{2, 1}, rc12{1, 2}, rc01{0, 1}, rc10{1, 0};
-    const float h1x = float(csize[0] - 1) / range[0];
-    const float h1y = float(csize[1] - 1) / range[1];
-    const float h1z = float(csize[2] - 1) / range[2];
-    const float h2x = h1x * h1x, h2y = h1y * h1y, h2z = h1z * h1z;
-    const float h3x = h1x * h2x, h3y = h1y * h2y, h3z = h1z * h2z;
-    const float h4x = h1x * h3x, h4y = h1y * h3y, h4z = h1z * h3z;
-    const double gs = 1.0 / double(float(h1x * h1y) * h1z);
-    const double wsum = wdiv + wrot, wdelta = 2 * (wdiv - wrot);
-    std::vector<float> P(9 * 9 * 9 * 6, 0.0f);
-    size_t pi = 0;
-    for (int z = -4; z <= 4; ++z) {
-        const double r00z = rc00.get(z), r01z = h1z * rc01.get(z), r11z = h2z * rc11.get(z);
-        const double r12z = h3z * rc12.get(z), r22z = h4z * rc22.get(z);
-        for (int y = -4; y <= 4; ++y) {
-            const double r00y = rc00.get(y), r01y = h1y * rc01.get(y), r10y = h1y * rc10.get(y);
-            const double r11y = h2y * rc11.get(y), r12y = h3y * rc12.get(y), r21y = h3y * rc21.get(y);
-            const double r22y = h4y * rc22.get(y);
-            for (int x = -4; x <= 4; ++x, ++pi) {
-                const double r00x = rc00.get(x), r01x = h1x * rc01.get(x), r10x = h1x * rc10.get(x);
-                const double r11x = h2x * rc11.get(x), r21x = h3x * rc21.get(x), r22x = h4x * rc22.get(x);
-                const double r200200 = r22x * r00y * r00z, r020020 = r00x * r22y * r00z;
-                const double r002002 = r00x * r00y * r22z, r110110 = r11x * r11y * r00z;
-                const double r101101 = r11x * r00y * r11z, r011011 = r00x * r11y * r11z;
-                const double vxx = gs * (r002002 * wrot + r011011 * 2.0 * wrot + r020020 * wrot +
-                                         r101101 * wsum + r110110 * wsum + r200200 * wdiv);
-                const double vyy = gs * (r002002 * wrot + r011011 * wsum + r020020 * wdiv +
-                                         r101101 * 2 * wrot + r110110 * wsum + r200200 * wrot);
-                const double vzz = gs * (r002002 * wdiv + r011011 * wsum + r020020 * wrot +
-                                         r101101 * wsum + r110110 * wrot * 2 + r200200 * wrot);
-                double vxy = 0, vxz = 0, vyz = 0;
-                if (wdelta != 0.0) {
-                    vxy = gs * wdelta * (r21x * r01y * r00z + r10x * r12y * r00z + r01x * r10y * r11z);
-                    vxz = gs * wdelta * (r21x * r00y * r01z + r10x * r11y * r01z + r10x * r00y * r12z);
-                    vyz = gs * wdelta * (r11x * r10y * r01z + r00x * r21y * r01z + r00x * r10y * r12z);
-                }
-                float *c = &P[pi * 6];
-                c[0] = float(vxx);
-                c[1] = float(vxy);
-                c[2] = float(vyy);
-                c[3] = float(vyz);
-                c[4] = float(vzz);
-                c[5] = float(vxz);
-            }
-        }
+    const double t = std::fabs(x);
+    if (t >= 2.0) return 0.0;
+    const double sgn = x < 0.0 ? -1.0 : 1.0;
+    if (t <= 1.0) {
+        if (p == 0) return (4.0 + t * t * (3.0 * t - 6.0)) / 6.0;
+        if (p == 1) return sgn * t * (1.5 * t - 2.0);
+        return 3.0 * t - 2.0;
     }
+    const double r = 2.0 - t;
+    if (p == 0) return r * r * r / 6.0;
+    if (p == 1) return -0.5 * sgn * r * r;
+    return r;
+}
+
+// J(p, q; s, t) without the factor h^(p+q), over the overlap of the two
+// supports inside [lo, hi] (R1)
+double overlap_integral(int p, int q, double s, double t, double lo, double hi)
+{
+    const double a = std::max(std::max(s, t) - 2.0, lo);
+    const double b = std::min(std::min(s, t) + 2.0, hi);
+    if (!(b > a)) return 0.0;
+    const int panels = int(8.0 * (b - a));
+    const double w = (b - a) / panels;
+    auto f = [&](double x) { return cubic_bspline_derivative(x - s, p) * cubic_bspline_derivative(x - t, q); };
+    double ends = f(a) + f(b), inner = 0.0, mid = 0.0;
+    for (int k = 0; k < panels; ++k) {
+        const double x = a + k * w;
+        if (k > 0) inner += f(x);
+        mid += f(x + 0.5 * w);
+    }
+    return (ends + 2.0 * inner + 4.0 * mid) * w / 6.0;
+}
+
+// h^k for k = 0..4 as float products (R2)
+void float_powers(float h, float hp[5])
+{
+    hp[0] = 1.0f;
+    for (int k = 1; k < 5; ++k) hp[k] = h * hp[k - 1];
+}
+
+// one term of a block entry: weight and the derivative orders at i and j
+struct PenaltyTerm {
+    double w;
+    int alpha[3];
+    int beta[3];
+};
+
+// the terms of block entry (c, cp), c <= cp, in a d-dimensional field
+std::vector<PenaltyTerm> divcurl_terms(int dim, int c, int cp, double wdiv, double wrot)
+{
+    std::vector<PenaltyTerm> terms;
+    auto orders = [](int a, int b, int o[3]) {
+        o[0] = o[1] = o[2] = 0;
+        ++o[a];
+        ++o[b];
+    };
+    if (c == cp) {
+        for (int a = 0; a < dim; ++a) {
+            PenaltyTerm t{wdiv, {0, 0, 0}, {0, 0, 0}};
+            orders(a, c, t.alpha);
+            orders(a, c, t.beta);
+            terms.push_back(t);
+            for (int b = 0; b < dim; ++b) {
+                if (b == c) continue;
+                PenaltyTerm r{wrot, {0, 0, 0}, {0, 0, 0}};
+                orders(a, b, r.alpha);
+                orders(a, b, r.beta);
+                terms.push_back(r);
+            }
+        }
+        return terms;
+    }
+    const double w = 2.0 * (wdiv - wrot);   // R3
+    if (w == 0.0) return terms;
+    for (int a = 0; a < dim; ++a) {
+        PenaltyTerm t{w, {0, 0, 0}, {0, 0, 0}};
+        orders(a, c, t.alpha);
+        orders(a, cp, t.beta);
+        if (c == 0 && cp == 1 && a == dim - 1) std::swap(t.alpha, t.beta);   // R4
+        terms.push_back(t);
+    }
+    return terms;
+}
+
+// the stored entries of a block: 3D (xx, xy, yy, yz, zz, xz), 2D (xx, yy, xy)
+constexpr int kEntries3[6][2] = {{0, 0}, {0, 1}, {1, 1}, {1, 2}, {2, 2}, {0, 2}};
+constexpr int kEntries2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
+
+}  // namespace
+
+std::vector<double> penalty3_cells(const int csize[3], const float range[3], double wdiv, double wrot)
+{
+    // J per axis, derivative pair and offset d = -4..4 over the whole
+    // overlap (R5), scaled by the float power of h (R2)
+    double J[3][3][3][9];
+    float hg = 1.0f;
+    for (int a = 0; a < 3; ++a) {
+        const float h = float(csize[a] - 1) / range[a];
+        float hp[5];
+        float_powers(h, hp);
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q)
+                for (int d = -4; d <= 4; ++d)
+                    J[a][p][q][d + 4] = double(hp[p + q]) * overlap_integral(p, q, 0.0, double(d), -1e30, 1e30);
+        hg = a == 0 ? h : hg * h;
+    }
+    const double gscale = 1.0 / double(hg);
+    std::vector<PenaltyTerm> terms[6];
+    for (int e = 0; e < 6; ++e) terms[e] = divcurl_terms(3, kEntries3[e][0], kEntries3[e][1], wdiv, wrot);
+    std::vector<double> P(size_t(9 * 9 * 9) * 6, 0.0);
+    for (int dz = 0; dz < 9; ++dz)
+        for (int dy = 0; dy < 9; ++dy)
+            for (int dx = 0; dx < 9; ++dx) {
+                const int d[3] = {dx, dy, dz};
+                double *cell = &P[(size_t(dz * 9 + dy) * 9 + dx) * 6];
+                for (int e = 0; e < 6; ++e) {
+                    double v = 0.0;
+                    for (const PenaltyTerm &t : terms[e]) {
+                        double prod = t.w;
+                        for (int a = 0; a < 3; ++a) prod *= J[a][t.alpha[a]][t.beta[a]][d[a]];
+                        v += prod;
+                    }
+                    cell[e] = gscale * v;
+                }
+            }
     return P;
 }
 
-// C2DPPDivcurlMatrixImpl::reset (mia/2d/ppmatrix.cc:182-243) with the
-// (skip, delta)-keyed CIntegralCache (ppmatrix.cc:113-172); cells grouped
-// by row i in list order (CSR).
+std::vector<float> build_penalty3(const int csize[3], const float range[3], double wdiv, double wrot)
+{
+    const std::vector<double> P = penalty3_cells(csize, range, wdiv, wrot);
+    return std::vector<float>(P.begin(), P.end());
+}
+
+void penalty2_cells(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
+                    std::vector<int> &col, std::vector<double> &val)
+{
+    const int n[2] = {csize[0], csize[1]};
+    // J per axis and derivative pair for the coefficient s and its
+    // neighbours t = s - 4 .. s + 3, clipped to [0, n_c] (R5)
+    std::vector<double> J[2];
+    auto jat = [&](int a, int p, int q, int s, int t) -> double {
+        return J[a][((size_t(p) * 3 + q) * n[a] + s) * 8 + (t - s + 4)];
+    };
+    float hg = 1.0f;
+    for (int a = 0; a < 2; ++a) {
+        const float h = float(n[a] - 1) / range[a];
+        float hp[5];
+        float_powers(h, hp);
+        J[a].assign(size_t(9) * n[a] * 8, 0.0);
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q)
+                for (int s = 0; s < n[a]; ++s)
+                    for (int t = std::max(0, s - 4); t < std::min(n[a], s + 4); ++t)
+                        J[a][((size_t(p) * 3 + q) * n[a] + s) * 8 + (t - s + 4)] =
+                            double(hp[p + q]) * overlap_integral(p, q, double(s), double(t), 0.0, double(n[a]));
+        hg = a == 0 ? h : hg * h;
+    }
+    const double gscale = 1.0 / double(hg);
+    std::vector<PenaltyTerm> terms[3];
+    for (int e = 0; e < 3; ++e) terms[e] = divcurl_terms(2, kEntries2[e][0], kEntries2[e][1], wd, wr);
+    const int nx = n[0], ny = n[1];
+    rowptr.assign(size_t(nx) * ny + 1, 0);
+    col.clear();
+    val.clear();
+    for (int l = 0; l < ny; ++l)
+        for (int k = 0; k < nx; ++k) {
+            for (int m2 = std::max(0, l - 4); m2 < std::min(l + 4, ny); ++m2)
+                for (int m1 = std::max(0, k - 4); m1 < std::min(k + 4, nx); ++m1) {
+                    const int s[2] = {k, l}, t[2] = {m1, m2};
+                    double v[3];
+                    for (int e = 0; e < 3; ++e) {
+                        double acc = 0.0;
+                        for (const PenaltyTerm &tm : terms[e]) {
+                            double prod = tm.w;
+                            for (int a = 0; a < 2; ++a) prod *= jat(a, tm.alpha[a], tm.beta[a], s[a], t[a]);
+                            acc += prod;
+                        }
+                        v[e] = gscale * acc;
+                    }
+                    if (v[0] == 0.0 && v[1] == 0.0 && v[2] == 0.0) continue;   // R6
+                    col.push_back(m1 + m2 * nx);
+                    val.push_back(v[0]);
+                    val.push_back(v[1]);
+                    val.push_back(v[2]);
+                }
+            rowptr[size_t(l) * nx + k + 1] = int(col.size());
+        }
+}
+
 void build_penalty2(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
                     std::vector<int> &col, std::vector<float> &val)
 {
-    struct Cache {
-        std::map<int, double> values;
-        double get(int s1, int s2, int d1, int d2, int range)
-        {
-            bool swapped = false;
-            if (s2 < s1) { swapped = true; std::swap(s1, s2); }
-            int delta = s2 - s1;
-            if (delta >= 4) return 0.0;
-            int skip = 0;
-            const int dlow = 2 - s1;
-            if (dlow > 0) {
-                skip = s2 - 2;
-                if (skip > 0) skip = 0;
-            } else {
-                const int dhigh = 2 + s2 - range;
-                if (dhigh > 0) skip = 2 + s1 - range;
-                if (skip < 0) skip = 0;
-            }
-            if (std::abs(skip) >= 4) return 0.0;
-            if (swapped) { delta = -delta; std::swap(s1, s2); }
-            const int index = skip * 8 + delta + 4;
-            auto pv = values.find(index);
-            if (pv != values.end()) return pv->second;
-            const double r = values[index] = integrate2(s1, s2, d1, d2, 0, range);
-            return r;
-        }
-    };
-    const int nx = csize[0], ny = csize[1];
-    const float h1x = float(nx - 1) / range[0], h1y = float(ny - 1) / range[1];
-    const double gs = 1.0 / double(h1x * h1y);
-    const float h2x = h1x * h1x, h2y = h1y * h1y, h3x = h1x * h2x, h3y = h1y * h2y;
-    const float h4x = h1x * h3x, h4y = h1y * h3y;
-    Cache rc22, rc21, rc01, rc12, rc10, rc00, rc11;
-    struct Cell { int i, j; float vx, vy, v12; };
-    std::vector<Cell> cells;
-    for (int l = 0; l < ny; ++l)
-        for (int n = std::max(0, l - 4); n < std::min(l + 4, ny); ++n) {
-            const double r00y = rc00.get(l, n, 0, 0, ny), r01y = h1y * rc01.get(l, n, 0, 1, ny);
-            const double r11y = h2y * rc11.get(l, n, 1, 1, ny), r21y = h3y * rc21.get(l, n, 2, 1, ny);
-            const double r22y = h4y * rc22.get(l, n, 2, 2, ny);
-            for (int k = 0; k < nx; ++k)
-                for (int m = std::max(0, k - 4); m < std::min(k + 4, nx); ++m) {
-                    const double r00x = rc00.get(k, m, 0, 0, nx), r01x = h1x * rc01.get(k, m, 0, 1, nx);
-                    const double r11x = h2x * rc11.get(k, m, 1, 1, nx), r21x = h3x * rc21.get(k, m, 2, 1, nx);
-                    const double r22x = h4x * rc22.get(k, m, 2, 2, nx);
-                    const double vx = gs * (wd * (r22x * r00y + r11x * r11y) + wr * (r11x * r11y + r00x * r22y));
-                    const double v12 = 2 * gs * (wd - wr) * (r21x * r01y + r01x * r21y);
-                    const double vy = gs * (wd * (r00x * r22y + r11x * r11y) + wr * (r22x * r00y + r11x * r11y));
-                    if (vx != 0.0 || v12 != 0.0 || vy != 0.0)
-                        cells.push_back({k + l * nx, m + n * nx, float(vx), float(vy), float(v12)});
-                }
-        }
-    std::stable_sort(cells.begin(), cells.end(), [](const Cell &a, const Cell &b) { return a.i < b.i; });
-    rowptr.assign(size_t(nx) * ny + 1, 0);
-    col.resize(cells.size());
-    val.resize(cells.size() * 4);
-    for (const Cell &c : cells) rowptr[c.i + 1]++;
-    for (size_t i = 0; i < size_t(nx) * ny; ++i) rowptr[i + 1] += rowptr[i];
-    for (size_t e = 0; e < cells.size(); ++e) {
-        col[e] = cells[e].j;
-        val[e * 4] = cells[e].vx;
-        val[e * 4 + 1] = cells[e].vy;
-        val[e * 4 + 2] = cells[e].v12;
-        val[e * 4 + 3] = 0.0f;
+    std::vector<double> v;
+    penalty2_cells(csize, range, wd, wr, rowptr, col, v);
+    // device layout: (xx, yy, xy, 0) per cell
+    val.assign(v.size() / 3 * 4, 0.0f);
+    for (size_t e = 0; e < v.size() / 3; ++e) {
+        val[e * 4] = float(v[e * 3]);
+        val[e * 4 + 1] = float(v[e * 3 + 1]);
+        val[e * 4 + 2] = float(v[e * 3 + 2]);
     }
 }
 

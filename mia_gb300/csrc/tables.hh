@@ -23,6 +23,14 @@ struct AxisHost {
 
 int csize_from_rate(int size, float rate);
 void build_axis(AxisHost &ax, int n, int nc, int tile);
+// divcurl penalty tables (see tables.cc).  3D: the 9^3 cells of offsets
+// d = i - j (index ((dz + 4) 9 + dy + 4) 9 + dx + 4), six entries each
+// (xx, xy, yy, yz, zz, xz).  2D: per coefficient i (row, CSR) the
+// coefficients j it couples with, three entries each (xx, yy, xy).
+std::vector<double> penalty3_cells(const int csize[3], const float range[3], double wdiv, double wrot);
+void penalty2_cells(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
+                    std::vector<int> &col, std::vector<double> &val);
+// the same rounded to float for the device; 2D cells padded to four floats
 std::vector<float> build_penalty3(const int csize[3], const float range[3], double wdiv, double wrot);
 void build_penalty2(const int csize[2], const float range[2], double wd, double wr, std::vector<int> &rowptr,
                     std::vector<int> &col, std::vector<float> &val);

@@ -1295,6 +1295,36 @@ double orc_simpson_integrate2(double s1, double s2, int deg1, int deg2, double x
     return integrate2(s1, s2, deg1, deg2, 1, x0, L);
 }
 
+void orc_divcurl_table3(const int csize[3], const float range[3], double wdiv, double wrot, double *out)
+{
+    PPMatrix3 m;
+    m.reset(csize, range, wdiv, wrot);
+    for (size_t c = 0; c < m.P.size(); ++c) {
+        const Cell3 &p = m.P[c];
+        double *o = out + c * 6;
+        o[0] = p.vxx; o[1] = p.vxy; o[2] = p.vyy; o[3] = p.vyz; o[4] = p.vzz; o[5] = p.vxz;
+    }
+}
+
+size_t orc_divcurl_cells2(const int csize[2], const float range[2], double wd, double wr, int *i, int *j,
+                          double *v, size_t cap)
+{
+    PPMatrix2 m;
+    m.reset(csize, range, wd, wr);
+    /* the cells grouped by row i in list order, as the reference's
+       evaluation visits them row by row */
+    std::vector<size_t> order(m.P.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return m.P[a].i < m.P[b].i; });
+    for (size_t k = 0; k < order.size() && k < cap; ++k) {
+        const Cell2 &p = m.P[order[k]];
+        i[k] = int(p.i);
+        j[k] = int(p.j);
+        v[3 * k] = p.vx; v[3 * k + 1] = p.vy; v[3 * k + 2] = p.v12;
+    }
+    return m.P.size();
+}
+
 void orc_gradient(const float *img, float *grad, int dim, const int size[3])
 {
     Pool pool;

@@ -52,6 +52,15 @@ double orc_divcurl_matrix(int dim, const int csize[3], const float range[3],
                           double wdiv, double wrot, const double *coeffs,
                           double *grad, int as_float, int mode);
 
+/* the divcurl P tables themselves (for checks of other builders): 3D the
+   9x9x9 cells of offsets i - j, six doubles each (xx, xy, yy, yz, zz, xz),
+   cell index (dx + 4) + 9 ((dy + 4) + 9 (dz + 4)); 2D the nonzero cells
+   (i, j, xx, yy, xy) grouped by row i; returns the number of cells, of
+   which at most `cap` are written. */
+void   orc_divcurl_table3(const int csize[3], const float range[3], double wdiv, double wrot, double *out);
+size_t orc_divcurl_cells2(const int csize[2], const float range[2], double wd, double wr, int *i, int *j,
+                          double *v, size_t cap);
+
 /* ---- one registration level (transform + image full cost + penalty) -- */
 typedef struct OrcLevel OrcLevel;
 
