@@ -158,19 +158,26 @@ mgr_status mgr_level_set_timing(mgr_level *lvl, int enable);
 mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4]);
 
 /* Spline adjoint (translate, 3D) for callers that cannot allocate device
-   memory: code running under CUDA stream capture, hosts that own all device
-   memory through their own arena, latency-bound callers that cannot afford
-   cudaMalloc's implicit synchronisation.  No counterpart in the reference.
-   The caller passes the force field (d_force: size[0]*size[1]*size[2]
-   voxels x 3 floats, device) and receives the negated transposed-spline
-   contraction in d_grad (csize product x 3 doubles, device), identical to
-   mgr_level_translate; it runs asynchronously on `stream` (NULL: the legacy
-   default stream) of the calling thread's current device and allocates
-   nothing.  Intermediates live in one fixed 16 MiB device array per GPU
-   (reserved when the library loads, held until exit); sizes needing more
-   are rejected with MGR_ERR_ARG.  The first call on a device looks up that
-   array's device address, so make it before any stream capture.  Calls
-   share the array: calls whose kernels overlap on the GPU race. */
+   memory.  No counterpart in the reference.  Such callers are hosts that
+   hand all device memory to their own pool or arena and forbid other
+   allocations, and latency-bound callers that cannot afford the implicit
+   device synchronisation of cudaMalloc/cudaFree.  The caller passes the
+   force field (d_force: size[0]*size[1]*size[2] voxels x 3 floats, device)
+   and receives the negated transposed-spline contraction in d_grad (csize
+   product x 3 doubles, device): bit for bit the result of
+   mgr_level_translate for the same sizes (the same per-axis rows and the
+   same three passes).  It runs asynchronously on `stream` (NULL: the legacy
+   default stream) of the calling thread's current device and calls no
+   allocating function.  Its intermediates live in one fixed 16 MiB device
+   array per GPU, which the CUDA runtime sets up when it first loads this
+   library's device code on that GPU (under lazy loading, the default, that
+   is the first call) and which stays reserved until the process exits;
+   sizes needing more are rejected with MGR_ERR_ARG.  The first call on a
+   device also looks up that array's device address (once per device), so
+   make the first call on each device outside any stream capture.  Calls
+   share the array and it keeps the last call's contents: calls whose
+   kernels overlap on the GPU (other streams, other host threads) race on
+   it and must be serialised by the caller. */
 mgr_status mgr_translate3d_noalloc(const int size[3], const int csize[3], const float *d_force,
                                    double *d_grad, void *stream);
 
@@ -302,13 +309,25 @@ mgr_status mgr_level_sync(mgr_level *lvl);
    one thread waits on a barrier that nothing completes, with the warp
    kernel's wait at a limit of 1024 tries.  *gave_up = 1 when the wait ended
    by its limit and raised its flag (the expected result); *us_per_try is
-   the time of one failed try, from which the production limit (2^20 tries)
-   takes its duration.  The device stays usable afterwards. */
+   the time of one failed try, read from the GPU's global nanosecond timer,
+   from which the production limit (2^20 tries) takes its duration.  The
+   device stays usable afterwards and the calling thread's current device is
+   restored. */
 mgr_status mgr_selftest_bounded_wait(int device, int *gave_up, double *us_per_try);
 
 /* Number of kernels this library has launched in the calling process
    (for launch accounting in benchmarks). */
 unsigned long long mgr_kernel_launch_count(void);
+
+/* Test aids for the out-of-memory paths (no counterpart in the reference,
+   whose allocations throw std::bad_alloc).  After mgr_debug_fail_allocation(k)
+   with k > 0, the k-th device or page-locked host allocation this library
+   makes from then on fails as an exhausted device would, and the call that
+   made it returns MGR_ERR_OOM; k = 0 disarms.  Process-wide.
+   mgr_allocation_count is the number of such allocations the library has
+   made so far in the process. */
+mgr_status mgr_debug_fail_allocation(long long k);
+unsigned long long mgr_allocation_count(void);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,8 @@ _vp = ctypes.c_void_p
 SIGNATURES = {
     "mgr_last_error": (ctypes.c_char_p, []),
     "mgr_kernel_launch_count": (ctypes.c_ulonglong, []),
+    "mgr_debug_fail_allocation": (ctypes.c_int, [ctypes.c_longlong]),
+    "mgr_allocation_count": (ctypes.c_ulonglong, []),
     "mgr_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                                  ctypes.POINTER(ctypes.c_double)]),
     "mgr_level_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.POINTER(_vp)]),

@@ -29,6 +29,37 @@ void count_launch_pause(bool paused) { g_capturing = paused; }
 static thread_local std::string g_err;
 void set_last_error(const std::string &msg) { g_err = msg; }
 
+// allocation accounting and failure injection (mgr_debug_fail_allocation)
+static std::atomic<unsigned long long> g_allocs{0};
+static std::atomic<long long> g_fail_in{0};   // 0: off; k: the k-th allocation from now fails
+
+static bool injected_allocation_failure()
+{
+    g_allocs.fetch_add(1, std::memory_order_relaxed);
+    long long k = g_fail_in.load();
+    while (k > 0)
+        if (g_fail_in.compare_exchange_weak(k, k - 1)) return k == 1;
+    return false;
+}
+
+cudaError_t dev_malloc_async(void **p, size_t bytes, cudaStream_t s)
+{
+    if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
+    return cudaMallocAsync(p, bytes, s);
+}
+
+cudaError_t dev_malloc(void **p, size_t bytes)
+{
+    if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_malloc_pinned(void **p, size_t bytes)
+{
+    if (injected_allocation_failure()) return cudaErrorMemoryAllocation;
+    return cudaMallocHost(p, bytes);
+}
+
 // phase trace (MGR_TRACE=1)
 namespace {
 struct PhaseSum {
@@ -228,6 +259,15 @@ const char *mgr_last_error(void) { return g_err.c_str(); }
 
 unsigned long long mgr_kernel_launch_count(void) { return g_launches.load(); }
 
+mgr_status mgr_debug_fail_allocation(long long k)
+{
+    if (k < 0) return fail(MGR_ERR_ARG, "mgr_debug_fail_allocation: k must be >= 0");
+    g_fail_in.store(k);
+    return MGR_OK;
+}
+
+unsigned long long mgr_allocation_count(void) { return g_allocs.load(); }
+
 mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream, mgr_level **out)
 {
     if (!desc || !out) return fail(MGR_ERR_ARG, "null argument");
@@ -292,6 +332,7 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         check_launch("level create");
     });
     if (st == MGR_OK) *out = L.release();
+    else mgr_level_destroy(L.release());   // buffers made so far, and a stream the level created
     return st;
 }
 

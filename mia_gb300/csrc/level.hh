@@ -65,7 +65,7 @@ struct DevBuf {
         if (count <= n && p) return;
         release();
         if (count == 0) return;
-        ck(cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), s), "cudaMallocAsync");
+        ck(dev_malloc_async(reinterpret_cast<void **>(&p), count * sizeof(T), s), "cudaMallocAsync");
         st = s;
         n = count;
     }
@@ -184,7 +184,7 @@ struct mgr_level {
     double *host_small_p = nullptr;
     double *host_small()
     {
-        if (!host_small_p) ck(cudaMallocHost(reinterpret_cast<void **>(&host_small_p), 4 * sizeof(double)),
+        if (!host_small_p) ck(host_malloc_pinned(reinterpret_cast<void **>(&host_small_p), 4 * sizeof(double)),
                               "cudaMallocHost");
         return host_small_p;
     }

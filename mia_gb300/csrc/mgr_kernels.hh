@@ -19,6 +19,14 @@ void count_launch(unsigned n = 1);
 int device_sm_count();
 void count_launch_pause(bool paused);
 
+// Every device and page-locked host allocation of the library goes through
+// these three, so that mgr_debug_fail_allocation can make a chosen one fail
+// as an out-of-memory would (the allocation-failure paths are tested
+// without exhausting a device).
+cudaError_t dev_malloc_async(void **p, size_t bytes, cudaStream_t s);
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t host_malloc_pinned(void **p, size_t bytes);
+
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
 // padded copy with the mirror fold applied in the halo (layout of coef_pad)
 void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st);

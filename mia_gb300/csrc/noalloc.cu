@@ -1,21 +1,20 @@
 // noalloc.cu — the spline adjoint (translate) for callers that cannot
 // allocate device memory.
 //
-// Some callers of this library cannot call cudaMalloc: code that runs while
-// a stream is being captured into a CUDA graph (allocation is not a stream
-// operation and is refused during capture), hosts that hand every byte of
-// device memory to their own arena and forbid outside allocation, and
-// latency-bound callers for whom cudaMalloc's implicit device
-// synchronisation is not acceptable.  mgr_translate3d_noalloc serves them:
-// the caller passes the force field and the gradient buffer, and every
-// intermediate (per-axis transposed spline rows and the two separable pass
-// buffers) lives in one fixed, file-scope device array.
+// Some callers of this library cannot call cudaMalloc: hosts that hand
+// every byte of device memory to their own pool or arena and forbid
+// allocations outside it, and latency-bound callers for whom the implicit
+// device synchronisation of cudaMalloc and cudaFree is not acceptable.
+// mgr_translate3d_noalloc serves them: the caller passes the force field
+// and the gradient buffer, and every intermediate (per-axis transposed
+// spline rows and the two separable pass buffers) lives in one fixed,
+// file-scope device array.
 //
 // The array is kNoAllocScratchBytes (16 MiB) on every GPU that loads this
-// library and stays reserved until the process exits.  All calls share it
-// and it keeps the contents of the last call; calls whose kernels overlap on
-// the GPU (different streams, or different host threads on one device)
-// race on it and must be serialised by the caller.
+// library's device code and stays reserved until the process exits.  All
+// calls share it and it keeps the contents of the last call; calls whose
+// kernels overlap on the GPU (different streams, or different host threads
+// on one device) race on it and must be serialised by the caller.
 #include <mutex>
 #include <string>
 
@@ -99,9 +98,13 @@ __global__ void k_noalloc_rows(int n, int nc, double scale, int *as, float *aw, 
         for (int k = 0; k < 4; ++k) aw[size_t(t) * 4 + k] = w[k];
     }
     if (t < nc) {
+        // the voxels i with |i scale + 1 - t| < 2: x grows with i, so the
+        // scan starts below the first of them and ends where x reaches 2
         int first = -1, len = 0;
-        for (int i = 0; i < n; ++i) {
+        const int i0 = max(0, int(floor((double(t) - 3.0) / scale)) - 1);
+        for (int i = i0; i < n; ++i) {
             const double x = row_x(i, scale, t);
+            if (x >= 2.0) break;
             if (fabs(x) < 2.0) {
                 if (first < 0) first = i;
                 if (b3_unfused(x) > 0) ++len;
@@ -158,8 +161,16 @@ extern "C" mgr_status mgr_translate3d_noalloc(const int size[3], const int csize
                        " bytes; use mgr_level_translate instead");
         return MGR_ERR_ARG;
     }
+    // an error left by earlier work of this thread is reported as such and
+    // not taken for a failure of this call's launches
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        set_last_error(std::string("mgr_translate3d_noalloc: a CUDA error from earlier work is pending on this "
+                                   "thread: ") + cudaGetErrorString(e));
+        return MGR_ERR_CUDA;
+    }
     void *base = nullptr;
-    cudaError_t e = scratch_on_current_device(&base);
+    e = scratch_on_current_device(&base);
     if (e != cudaSuccess) {
         set_last_error(std::string("mgr_translate3d_noalloc: scratch address: ") + cudaGetErrorString(e));
         return MGR_ERR_CUDA;

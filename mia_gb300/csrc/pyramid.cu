@@ -294,7 +294,7 @@ void scale_axis(const float *in, float *out, const AxisPlan &p, int n_in, int n_
     std::memcpy(blob.data() + o_idx, p.idx.data(), p.idx.size() * sizeof(int4));
     std::memcpy(blob.data() + o_wts, wts.data(), wts.size() * sizeof(float4));
     unsigned char *d = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
     ck(cudaMemcpyAsync(d, blob.data(), bytes, cudaMemcpyHostToDevice, st), "H2D");
     // lines per block: at most 64 and 96 KB of staged lines, fewer while
     // the launch would have less than two blocks per SM (the block's line
@@ -371,7 +371,7 @@ bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_s
 {
     const int nb = pair_sum_blocks(n);
     double *d_part = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d_part), size_t(nb) * 2 * sizeof(double), st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&d_part), size_t(nb) * 2 * sizeof(double), st), "cudaMallocAsync");
     k_pair_sums<<<nb, 256, 0, st>>>(d_src, d_ref, n, d_part);
     count_launch();
     std::vector<double> part(size_t(nb) * 2);
@@ -409,7 +409,7 @@ std::vector<char> normalize_pairs(const std::vector<const float *> &src, const s
     }
     const size_t o_part = ((sizeof(NormJob) * np + 255) / 256) * 256;
     unsigned char *d = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d), o_part + nparts * sizeof(double), st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&d), o_part + nparts * sizeof(double), st), "cudaMallocAsync");
     double *d_part = reinterpret_cast<double *>(d + o_part);
     size_t off = 0;
     std::vector<size_t> at(np);
@@ -456,7 +456,7 @@ void scale_image(const float *d_in, const int in_size[3], float *d_out, const in
             throw std::invalid_argument("scale: only downscaling to sizes >= 2 is supported");
     // x: lines = rows (y, z)
     float *t1 = nullptr, *t2 = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&t1), size_t(mx) * ny * nz * sizeof(float), st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&t1), size_t(mx) * ny * nz * sizeof(float), st), "cudaMallocAsync");
     const AxisPlan px = plan_axis(nx, mx);
     const AxisPlan py = plan_axis(ny, my);
     // (C1DScalar copies when the size does not change on an axis)
@@ -467,7 +467,7 @@ void scale_image(const float *d_in, const int in_size[3], float *d_out, const in
         cudaFreeAsync(t1, st);
         return;
     }
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&t2), size_t(mx) * my * nz * sizeof(float), st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&t2), size_t(mx) * my * nz * sizeof(float), st), "cudaMallocAsync");
     // y: lines = (x, z): per plane z, mx lines of stride 1, element stride mx
     scale_axis(t1, t2, py, ny, my, mx * nz, 1, size_t(mx), 1, size_t(mx), mx, size_t(mx) * ny, size_t(mx) * my, st);
     // z: lines = (x, y): mx*my lines, element stride mx*my

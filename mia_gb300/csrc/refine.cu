@@ -240,7 +240,7 @@ void refine_params_device(int dim, const std::vector<RefineJobSpec> &specs, cuda
     const size_t o_sc = up(o_ti + sizeof(int) * tap_ints);
     const size_t bytes = o_sc + sizeof(double) * scratch;
     unsigned char *d = nullptr;
-    ck(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
+    ck(dev_malloc_async(reinterpret_cast<void **>(&d), bytes, st), "cudaMallocAsync");
     std::vector<unsigned char> host(o_sc, 0);
     size_t pi = 0, pd = 0, ps = 0;
     for (int j = 0; j < nj; ++j) {
@@ -344,6 +344,9 @@ extern "C" mgr_status mgr_refine_coefficients_device(int dim, const int nc_old[3
     } catch (const std::invalid_argument &e) {
         set_last_error(e.what());
         return MGR_ERR_ARG;
+    } catch (const std::bad_alloc &) {
+        set_last_error("mgr_refine_coefficients_device: device allocation failed");
+        return MGR_ERR_OOM;
     } catch (const std::exception &e) {
         set_last_error(e.what());
         return MGR_ERR_CUDA;

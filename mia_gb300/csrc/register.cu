@@ -211,8 +211,8 @@ extern "C" mgr_status mgr_scale_image(int dim, const int in_size[3], const float
         ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
         const size_t ni = size_t(in_size[0]) * in_size[1] * (dim == 3 ? in_size[2] : 1);
         const size_t no = size_t(out_size[0]) * out_size[1] * (dim == 3 ? out_size[2] : 1);
-        ck(cudaMalloc(&d_in, ni * sizeof(float)), "cudaMalloc");
-        ck(cudaMalloc(&d_out, no * sizeof(float)), "cudaMalloc");
+        ck(dev_malloc(reinterpret_cast<void **>(&d_in), ni * sizeof(float)), "cudaMalloc");
+        ck(dev_malloc(reinterpret_cast<void **>(&d_out), no * sizeof(float)), "cudaMalloc");
         ck(cudaMemcpyAsync(d_in, in, ni * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
         scale_image(d_in, in_size, d_out, out_size, dim, st);
         ck(cudaMemcpyAsync(out, d_out, no * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H");
@@ -224,11 +224,12 @@ extern "C" mgr_status mgr_scale_image(int dim, const int in_size[3], const float
         if (st) cudaStreamDestroy(st);
         return MGR_ERR_ARG;
     } catch (const std::exception &e) {
-        set_last_error(e.what());
+        const bool oom = dynamic_cast<const std::bad_alloc *>(&e) != nullptr;
+        set_last_error(oom ? "mgr_scale_image: device allocation failed" : e.what());
         cudaFree(d_in);
         cudaFree(d_out);
         if (st) cudaStreamDestroy(st);
-        return MGR_ERR_CUDA;
+        return oom ? MGR_ERR_OOM : MGR_ERR_CUDA;
     }
     cudaFree(d_in);
     cudaFree(d_out);
@@ -249,7 +250,7 @@ extern "C" mgr_status mgr_normalize_pair(const float *src, const float *ref, siz
     try {
         ck(cudaSetDevice(device), "cudaSetDevice");
         ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
-        for (auto &p : d) ck(cudaMalloc(&p, n * sizeof(float)), "cudaMalloc");
+        for (auto &p : d) ck(dev_malloc(reinterpret_cast<void **>(&p), n * sizeof(float)), "cudaMalloc");
         ck(cudaMemcpyAsync(d[0], src, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
         ck(cudaMemcpyAsync(d[1], ref, n * sizeof(float), cudaMemcpyHostToDevice, st), "H2D");
         const bool ok = normalize_pair(d[0], d[1], n, d[2], d[3], st, mean, sigma);
@@ -259,6 +260,9 @@ extern "C" mgr_status mgr_normalize_pair(const float *src, const float *ref, siz
             ck(cudaMemcpyAsync(ref_out, d[3], n * sizeof(float), cudaMemcpyDeviceToHost, st), "D2H");
         }
         ck(cudaStreamSynchronize(st), "sync");
+    } catch (const std::bad_alloc &) {
+        set_last_error("mgr_normalize_pair: device allocation failed");
+        status = MGR_ERR_OOM;
     } catch (const std::exception &e) {
         set_last_error(e.what());
         status = MGR_ERR_CUDA;

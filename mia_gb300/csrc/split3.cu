@@ -173,6 +173,8 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     __shared__ int boxs[8];               // staged, xs, ylo, zbase, nplanes, span, w4, rows
     __shared__ __align__(8) unsigned long long mbar[RING_N];
     __shared__ unsigned rdone[RING_N];    // warps done with the ring slot's current plane
+    __shared__ int nissued;               // planes whose copies were issued
+    __shared__ volatile int ring_failed;  // a wait of this block gave up
     __shared__ bool is_last;
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
@@ -366,7 +368,11 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         // fixed-point floor may round p up to the next integer, one more
         // row / column / plane on the upper side
         const float big = 1.0e6f;
-        bool ok = a.has_tmap != 0;
+        // once a wait of this launch has given up (the flag the host reads
+        // afterwards), later blocks read their taps from global memory, so
+        // that a stalled copy engine costs one wait limit per launch, not
+        // one per block
+        bool ok = a.has_tmap != 0 && *(volatile unsigned *)&a.counters[6] == 0u;
 #pragma unroll
         for (int c = 0; c < 3; ++c) ok = ok && fabsf(ulo[c]) < big && fabsf(uhi[c]) < big;
         int xs = 0, xe = 0, ylo = 0, yhi = 0, dzl = 0, dzh = 0;
@@ -390,8 +396,12 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         boxs[5] = dzh - dzl + 1;
         boxs[6] = RING_X;
         boxs[7] = yhi - ylo + 1;
-        if (ok)
+        nissued = 0;
+        ring_failed = 0;
+        if (ok) {
             for (int k = 0; k < min(boxs[4], RING_N); ++k) issue_plane(k);
+            nissued = min(boxs[4], RING_N);
+        }
     }
     __syncthreads();
 
@@ -416,14 +426,17 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         if (ez > 1) r1 = __ldg(rin + nxy);
         if (ez > 2) r2 = __ldg(rin + 2 * nxy);
     }
-    int issued = staged ? min(nplanes, RING_N) : 0;
     for (int t = 0; t < ez; ++t) {
         advance(t);
         if (ring_ok) {
-            // the planes of this step (t .. t + span - 1) must have arrived
+            // the planes of this step (t .. t + span - 1) must have arrived;
+            // after any thread of the block gave up, none waits again
             while (kwait <= t + span - 1) {
-                if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) {
-                    atomicOr(&a.counters[6], 1u);
+                if (ring_failed || !mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) {
+                    if (!ring_failed) {
+                        ring_failed = 1;
+                        atomicOr(&a.counters[6], 1u);
+                    }
                     ring_ok = false;
                     break;
                 }
@@ -474,9 +487,10 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
                 __threadfence_block();
                 if (atomicAdd(&rdone[slot], 1u) == unsigned(NT3 / 32 - 1)) {
                     rdone[slot] = 0;
-                    if (ring_ok) {
+                    if (ring_ok && !ring_failed) {
                         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
                         issue_plane(t + RING_N);
+                        atomicAdd(&nissued, 1);
                     }
                 }
             }
@@ -485,10 +499,15 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     if (staged) __syncthreads();   // every warp is done with the ring
     if (staged && tid == 0) {
         // copies still in flight (only after a wait gave up) are waited for
-        // before the block's shared memory is released
-        issued = nplanes;
+        // before the block's shared memory is released: only the planes that
+        // were issued, and within one wait limit in total (a plane whose
+        // wait gives up ends the drain)
+        const int issued = nissued;
         while (kwait < issued) {
-            if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) break;
+            if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) {
+                atomicOr(&a.counters[6], 1u);
+                break;
+            }
             ++kwait;
         }
     }
@@ -1187,18 +1206,26 @@ void launch_gather3_batch(const EvalArgs *args, const int2 *items, int nitems, c
 // Self-test of the bounded wait: one thread waits on phase 0 of an mbarrier
 // that nothing arrives at (no copy is in flight), with the warp kernel's
 // wait at a limit of SELFTEST_TRIES tries; it must give up and raise the
-// flag, and the clock cycles it spent give the time of one failed try.
+// flag, and the global timer (nanoseconds, independent of the SM clock)
+// gives the time of one failed try.
 namespace {
 constexpr int SELFTEST_TRIES = 1024;
 
-__global__ void k_bounded_wait_selftest(unsigned *flag, long long *cycles)
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__global__ void k_bounded_wait_selftest(unsigned *flag, long long *ns)
 {
     __shared__ __align__(8) unsigned long long mb;
     const unsigned a = mgr::smem_u32(&mb);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
-    const long long t0 = clock64();
+    const unsigned long long t0 = global_ns();
     if (!mgr::mbar_wait<SELFTEST_TRIES>(a, 0u)) atomicOr(flag, 1u);
-    *cycles = clock64() - t0;
+    *ns = (long long)(global_ns() - t0);
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(a) : "memory");
 }
 }  // namespace
@@ -1209,30 +1236,31 @@ extern "C" mgr_status mgr_selftest_bounded_wait(int device, int *gave_up, double
         mgr::set_last_error("mgr_selftest_bounded_wait: null argument");
         return MGR_ERR_ARG;
     }
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
     unsigned *flag = nullptr;
-    long long *cycles = nullptr;
+    long long *ns = nullptr;
     unsigned f = 0;
-    long long c = 0;
-    int khz = 0;
-    cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaMalloc(&flag, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMalloc(&cycles, sizeof(long long));
+    long long t = 0;
+    if (e == cudaSuccess) e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = mgr::dev_malloc(reinterpret_cast<void **>(&flag), sizeof(unsigned));
+    if (e == cudaSuccess) e = mgr::dev_malloc(reinterpret_cast<void **>(&ns), sizeof(long long));
     if (e == cudaSuccess) e = cudaMemset(flag, 0, sizeof(unsigned));
     if (e == cudaSuccess) {
-        k_bounded_wait_selftest<<<1, 1>>>(flag, cycles);
+        k_bounded_wait_selftest<<<1, 1>>>(flag, ns);
         mgr::count_launch();
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(&f, flag, sizeof f, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(&c, cycles, sizeof c, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device);
+    if (e == cudaSuccess) e = cudaMemcpy(&t, ns, sizeof t, cudaMemcpyDeviceToHost);
     cudaFree(flag);
-    cudaFree(cycles);
+    cudaFree(ns);
+    cudaSetDevice(prev);   // the caller's current device is left as it was
     if (e != cudaSuccess) {
         mgr::set_last_error(std::string("mgr_selftest_bounded_wait: ") + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? MGR_ERR_OOM : MGR_ERR_CUDA;
     }
     *gave_up = f ? 1 : 0;
-    *us_per_try = khz > 0 ? double(c) / (double(khz) * 1e-3) / SELFTEST_TRIES : 0.0;
+    *us_per_try = double(t) * 1e-3 / SELFTEST_TRIES;
     return MGR_OK;
 }

@@ -111,14 +111,76 @@ def cohort_pairs(npairs, warp, rate=8.0, seed=5000):
     field (knot spacing 8, N(0,2) clipped to 4 voxels) and multiplied by a
     bias field (degree-2 exp polynomial, N(0,0.1)).  `warp(image, rate,
     seed)` applies the random deformation."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
     rng = np.random.default_rng(seed)
-    pairs = []
+    sizes = []
     for p in range(npairs):
         sx = int(rng.choice(np.arange(96, 225, 16)))
         sy = int(rng.choice(np.arange(96, 225, 16)))
         sz = int(rng.choice(np.arange(96, 161, 16)))
-        ref = blob_phantom((sz, sy, sx), 40, sigma=(4.0, 16.0), seed=seed + 100 + p)
+        sizes.append((sz, sy, sx))
+
+    def make(p):   # every pair from its own seeds: the threads' order does not matter
+        ref = blob_phantom(sizes[p], 40, sigma=(4.0, 16.0), seed=seed + 100 + p)
         mov = warp(ref, rate, seed + 1000 + p)
         mov = (mov * bias_field(mov.shape, 0.1, seed=seed + 2000 + p)).astype(np.float32)
-        pairs.append((mov, ref))
-    return pairs
+        return mov, ref
+    with ThreadPoolExecutor(max(1, min(8, os.cpu_count() or 1))) as ex:
+        return list(ex.map(make, range(npairs)))
+
+
+def _csize(n, rate):
+    """coefficient count per axis of a spline transformation of `n` voxels
+    at `rate`: floor((n - 1 + rate) / rate) in float, plus the border"""
+    return int(np.float32(np.float32(n - 1) + np.float32(rate)) / np.float32(rate)) + 2
+
+
+def _axis_weights(n, nc):
+    """dense (n x nc) matrix of the cubic B-spline weights of the
+    coefficients at the voxel coordinates i (nc - 3) / (n - 1) + 1"""
+    x = np.arange(n, dtype=np.float64) * ((nc - 3) / (n - 1.0)) + 1.0
+    t = np.abs(x[:, None] - np.arange(nc, dtype=np.float64)[None, :])
+    w = np.where(t < 1.0, (4.0 + t * t * (3.0 * t - 6.0)) / 6.0, np.where(t < 2.0, (2.0 - t) ** 3 / 6.0, 0.0))
+    return w
+
+
+def spline_field_params(shape, rate, sigma, clip, seed):
+    """random coefficients (N(0, sigma) clipped to +-clip) of a spline
+    transformation at `rate` for an image of `shape` ([z,] y, x); returns
+    the coefficient grid [.., dim] (x component first)"""
+    dim = len(shape)
+    cs = [_csize(n, rate) for n in shape]
+    return spline_params(int(np.prod(cs)), dim, sigma, clip, seed=seed).reshape(tuple(cs) + (dim,))
+
+
+def spline_warp_host(img, coeffs):
+    """img sampled at x - u(x), u the cubic B-spline field of `coeffs`
+    ([.., dim] on the coefficient grid of img's shape), with cubic B-spline
+    interpolation and mirror boundary (scipy), in float32.  Used to make the
+    benchmarks' moving images on the host, identically for every arm."""
+    from scipy import ndimage
+    shape = img.shape
+    dim = len(shape)
+    W = [_axis_weights(n, c) for n, c in zip(shape, coeffs.shape[:dim])]
+    coords = []
+    for k in range(dim):
+        u = coeffs[..., dim - 1 - k]          # component of array axis k (x is the last axis)
+        for ax in range(dim):
+            u = np.tensordot(W[ax], u, axes=([1], [ax]))
+            u = np.moveaxis(u, 0, ax)
+        grid = np.arange(shape[k], dtype=np.float64).reshape([-1 if a == k else 1 for a in range(dim)])
+        coords.append((grid - u).astype(np.float32))
+    out = ndimage.map_coordinates(img.astype(np.float64), np.array(coords), order=3, mode="mirror")
+    return out.astype(np.float32)
+
+
+def host_warp_factory(dim):
+    """warp(image, rate, seed): the random deformation of the benchmark
+    workloads (2D: N(0, 1.5) clipped to 3 px; 3D: N(0, 2) clipped to 4
+    voxels), applied on the host"""
+    sig, clip = (1.5, 3.0) if dim == 2 else (2.0, 4.0)
+
+    def warp(img, rate, seed):
+        return spline_warp_host(img, spline_field_params(img.shape, rate, sig, clip, seed))
+    return warp

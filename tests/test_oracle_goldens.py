@@ -241,3 +241,120 @@ def test_divcurl_penalty_plugin_sign_and_weight(goldens):
     np.testing.assert_allclose(gp, g["grad_factor"] * mg.ravel(), rtol=g["tol_pct"] / 100, atol=1e-300)
     ci, cpv = lvl.value(coef.ravel())
     assert close_pct(cpv, g["weight"] * O.divcurl_matrix(coef, rng_, 1.0, 1.0, with_grad=False, mode=1), 1e-6)
+
+
+# ---- 2D -----------------------------------------------------------------
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import golden2d  # noqa: E402
+
+
+@pytest.mark.parametrize("prec", [O.PREC_REF, O.PREC_F64])
+def test_splines_transform_shift_2d(goldens, prec):
+    g = goldens["test_splines_transform_2d"]
+    n = g["size"]
+    img = np.array(g["src"], np.float32).reshape(n[1], n[0])
+    lvl = O.Level(tuple(n), csize=tuple(g["coeff_size"]), precision=prec)
+    lvl.set_images(img, img)
+    w = lvl.warp(np.tile(np.array(g["shift"]), lvl.nparams // 2))
+    want = np.array(g["ref"], np.float32).reshape(n[1], n[0])
+    for got, exp in zip(w.ravel(), want.ravel()):
+        if exp > g["compare_if_above"] or got > g["compare_if_above"]:
+            assert close_pct(got, exp, g["tol_pct"])
+
+
+def test_splines_translate_constant_force_2d(goldens):
+    g = goldens["test_splines_translate_2d"]
+    r = g["range"]
+    lvl = O.Level(tuple(r), csize=tuple(g["coeff_size"]))
+    force = np.broadcast_to(np.array(g["force"], np.float32), (r[1], r[0], 2))
+    cs = lvl.csize
+    scale = np.prod([(r[i] - 1.0) / (cs[i] - 1 - 2) for i in range(2)])
+    gr = lvl.translate(force).reshape(cs[1], cs[0], 2)
+    inner = gr[4:cs[1] - 3, 4:cs[0] - 3].reshape(-1, 2)
+    for k in range(2):
+        want = g["expect_scaled"][k] * scale
+        assert np.all(np.abs(inner[:, k] - want) <= g["tol_pct"] / 100 * abs(want))
+
+
+def test_splines_prefix_iterator_2d(goldens):
+    """the transformation built from the prefiltered fixture field
+    reproduces the field at every pixel: x - T(x) = f(x)"""
+    g = goldens["test_splinestransform_prefix_iterator_2d"]
+    r = g["range"]
+    lvl = O.Level(tuple(r), csize=tuple(g["coeff_size"]))
+    z = np.zeros((r[1], r[0]), np.float32)
+    lvl.set_images(z, z)
+    u = lvl.displacement(golden2d.fixture_coefficients(g).ravel())
+    X, Y = np.meshgrid(np.arange(r[0]), np.arange(r[1]))
+    fx, fy = golden2d.fixture_field(g, X, Y)
+    for got, want in ((u[..., 0], fx), (u[..., 1], fy)):
+        m = (np.abs(want) > g["check_if_above"]) & (np.abs(got) > g["check_if_above"])
+        assert np.all(np.abs(got[m] - want[m]) <= g["tol_pct"] / 100 * np.abs(want[m]))
+
+
+def test_spline_c_rate_create_2d(goldens):
+    g = goldens["test_spline_c_rate_create_2d"]
+    lvl = O.Level(tuple(g["size"]), rate=tuple(g["c_rate"]))
+    assert list(lvl.csize) == g["coeff_size"]
+    z = np.zeros(tuple(g["size"][::-1]), np.float32)
+    lvl.set_images(z, z)
+    assert not np.any(lvl.displacement(np.zeros(lvl.nparams)))
+
+
+def _ppm_cases(goldens, with_checks):
+    return [(k, v) for k, v in goldens["divcurl_matrix_2d"].items() if ("checks" in v) == with_checks]
+
+
+def test_divcurl_matrix_2d_values(goldens):
+    """analytic values of the 2D divcurl matrix on divergence-only,
+    curl-only and exp(-r^2) fields, applied with the cubic kernel of the
+    registration path (the cases written for bspline:d=4 keep their field,
+    value and tolerance)"""
+    for name, c in _ppm_cases(goldens, True):
+        coeffs, fr = golden2d.ppmatrix_coefficients(c)
+        for chk in c["checks"]:
+            v = O.divcurl_matrix(coeffs, fr, chk["wdiv"], chk["wrot"], with_grad=False, as_float=False, mode=1)
+            if chk["expect"] == "zero":
+                assert close_pct(1.0 + v, 1.0, chk["tol_pct"]), (name, chk, v)
+            else:
+                want = {"6*pi": 6 * math.pi, "4*pi": 4 * math.pi}[chk["expect"]]
+                assert close_pct(v, want, chk["tol_pct"]), (name, chk, v)
+
+
+@pytest.mark.parametrize("name", ["test_divergence_expm2_bspline3_grad", "test_rotation_expm2_bspline3_grad",
+                                  "test_divergence_expm2_bspline3_grad_noiso",
+                                  "test_rotation_expm2_bspline3_grad_noiso"])
+def test_divcurl_matrix_2d_gradient_fd(goldens, name):
+    c = goldens["divcurl_matrix_2d"][name]
+    coeffs, fr = golden2d.ppmatrix_coefficients(c)
+    _, grad = O.divcurl_matrix(coeffs, fr, c["wdiv"], c["wrot"], with_grad=True, as_float=False, mode=0)
+    flat, gflat = coeffs.reshape(-1), grad.reshape(-1)
+    d = c["delta"]
+    for i in range(flat.size):
+        cc = flat.copy()
+        cc[i] += d
+        vp = O.divcurl_matrix(cc.reshape(coeffs.shape), fr, c["wdiv"], c["wrot"], with_grad=False, as_float=False,
+                              mode=1)
+        cc[i] -= 2 * d
+        vm = O.divcurl_matrix(cc.reshape(coeffs.shape), fr, c["wdiv"], c["wrot"], with_grad=False, as_float=False,
+                              mode=1)
+        fd = (vp - vm) / (2 * d)
+        if abs(fd) > c["check_if_abs_above"]:
+            assert close_pct(gflat[i], fd, c["tol_pct"]), (i, gflat[i], fd)
+
+
+def test_divcurl_penalty_2d_values(goldens):
+    """the 2D divcurl penalty plugin: weight * value = 6 pi / 3 pi on the
+    divergence-only (curl-only) field with weight, div and curl scaled"""
+    for name, c in goldens["divcurl_penalty_2d"].items():
+        coeffs = golden2d.penalty_coefficients(c)
+        n = c["size"]
+        size = tuple(int(v) for v in c["range"])
+        lvl = O.Level(size, csize=tuple(n), penalty_weight=c["weight"], div=c["div"], curl=c["curl"])
+        z = np.zeros(size[::-1], np.float32)
+        lvl.set_images(z, z)
+        _, cp = lvl.value(coeffs.ravel())
+        assert close_pct(cp, c["value_over_pi"] * math.pi, c["tol_pct"]), (name, cp)
