@@ -255,10 +255,14 @@ def oracle_pairs_per_s(w, pairs, seconds, threads):
 
 
 def oracle_final_costs(w, pairs, workers):
-    """per pair: the oracle's final cost, and how far it moves when the
-    moving image is perturbed at float rounding level (relative 1e-7,
-    seeded): the spread of the registration trajectory itself.  Pairs run
-    in parallel host threads, one thread per registration."""
+    """per pair, three registrations by the oracle: at the reference's
+    precision; the same with the moving image perturbed at float rounding
+    level (relative 1e-7, seeded); and with every evaluation in FP64.  The
+    last two measure how sensitive the pair's registration trajectory is:
+    the minimizer's accept/reject decisions compare costs, and the
+    reference sums the 2D cost in float (its force pass,
+    mia/2d/fullcost/image.cc:100), so rounding alone can move the final
+    cost.  Pairs run in parallel host threads, one thread per registration."""
     from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle as O
     mo = O.minimizer(w["minimizer"], maxiter=w["maxiter"], step=0.1)
@@ -270,34 +274,40 @@ def oracle_final_costs(w, pairs, workers):
         rng = np.random.default_rng(1 + k)
         m2 = (mov * (1 + 1e-7 * rng.standard_normal(mov.shape))).astype(np.float32)
         f1 = O.register(m2, ref, w["rate"], w["levels"], mo, **kw)[2]
-        return f0, abs(f1 - f0)
+        f64 = O.register(mov, ref, w["rate"], w["levels"], mo, precision=O.PREC_F64, **kw)[2]
+        return f0, abs(f1 - f0), f64
     with ThreadPoolExecutor(max(1, workers)) as ex:
         return list(ex.map(one, range(len(pairs))))
 
 
 def final_cost_report(res, plain_out, oracle):
     """final costs of the batched path against the plain per-pair GPU path
-    and, when given, against the oracle with its perturbation spread: a
-    pair passes when it is within 1e-4 relative or within 3x the oracle's
-    own spread"""
+    and, when given, against the oracle: a pair passes when its final cost
+    is within 1e-4 relative of the oracle's at the reference's precision,
+    or no further from it than the oracle's own FP64 run or 3x the
+    oracle's spread under a 1e-7 perturbation of the moving image (the
+    trajectory's sensitivity to rounding, measured per pair)"""
     rel = [abs(r[2] - o[2]) / max(abs(o[2]), 1e-300) for r, o in zip(res, plain_out)]
     rep = {"vs_plain_per_pair": {"max": float(max(rel)), "median": float(np.median(rel)),
                                  "pairs_within_1e-4": int(sum(1 for r in rel if r <= 1e-4)), "pairs": len(rel)}}
     if oracle:
         per = []
-        ok_b = ok_p = 0
-        for k, ((fo, spread), r, q) in enumerate(zip(oracle, res, plain_out)):
-            tol = max(1e-4 * abs(fo), 3 * spread)
+        ok_b = ok_p = in_b = 0
+        for k, ((fo, spread, f64), r, q) in enumerate(zip(oracle, res, plain_out)):
+            tol = max(1e-4 * abs(fo), 3 * spread, abs(f64 - fo))
             db, dp = abs(r[2] - fo), abs(q[2] - fo)
             ok_b += db <= tol
             ok_p += dp <= tol
-            per.append({"pair": k, "batched": r[2], "plain": q[2], "oracle": fo, "oracle_spread": spread,
-                        "batched_rel": db / abs(fo), "plain_rel": dp / abs(fo)})
-        rep["vs_oracle"] = {"rule": "|final - oracle| <= max(1e-4 |oracle|, 3 x oracle spread under a 1e-7 "
-                                    "perturbation of the moving image)",
+            in_b += db <= 1e-4 * abs(fo) or abs(r[2] - f64) <= 1e-4 * abs(f64)
+            per.append({"pair": k, "batched": r[2], "plain": q[2], "oracle": fo, "oracle_f64": f64,
+                        "oracle_perturbation_spread": spread, "batched_rel": db / abs(fo),
+                        "batched_rel_vs_f64": abs(r[2] - f64) / abs(f64), "plain_rel": dp / abs(fo)})
+        rep["vs_oracle"] = {"rule": "|final - oracle| <= max(1e-4 |oracle|, |oracle_f64 - oracle|, 3 x oracle spread "
+                                    "under a 1e-7 perturbation of the moving image)",
                             "batched_pairs_passing": int(ok_b), "plain_pairs_passing": int(ok_p), "pairs": len(per),
+                            "batched_within_1e-4_of_oracle_or_oracle_f64": int(in_b),
                             "max_batched_rel": float(max(p["batched_rel"] for p in per)),
-                            "max_oracle_spread_rel": float(max(p["oracle_spread"] / abs(p["oracle"]) for p in per)),
+                            "max_batched_rel_vs_f64": float(max(p["batched_rel_vs_f64"] for p in per)),
                             "per_pair": per}
     return rep
 

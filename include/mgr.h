@@ -90,6 +90,18 @@ mgr_status mgr_level_destroy(mgr_level *lvl);
    mia/3d/transform/spline.cc:414-418). */
 mgr_status mgr_level_csize(const mgr_level *lvl, int csize[3], size_t *nparams);
 
+/* A new coefficient grid for the level's images (kept, with their
+   prefiltered coefficients): the spline tables and the divcurl table are
+   rebuilt for `csize` (dim entries, each > 3).  Follows the transformation
+   where its grid changes while the image size stays: the coefficient grid
+   that C3DSplineTransformation::refine grows within a level
+   (mia/3d/transform/spline.cc:360-396) and the coarser grid that upscale
+   keeps for the next level's size (:399-412, before that level's
+   set_size).  A grid equal to the current one changes nothing.  Returns
+   after the rebuild; parameters and gradients of later calls have the new
+   size. */
+mgr_status mgr_level_set_grid(mgr_level *lvl, const int csize[3]);
+
 /* Replaces: C3DImageFullCost::do_reinit + TCost::set_reference
    (mia/3d/fullcost/image.cc:112-128, mia/core/cost.cxx:43-48) and the
    interpolator prefilter (mia/3d/interpolator.cxx:98-164), done once here

@@ -29,6 +29,7 @@ SIGNATURES = {
     "mgr_level_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
     "mgr_level_destroy": (ctypes.c_int, [_vp]),
     "mgr_level_csize": (ctypes.c_int, [_vp, _ip, ctypes.POINTER(ctypes.c_size_t)]),
+    "mgr_level_set_grid": (ctypes.c_int, [_vp, _ip]),
     "mgr_level_set_images": (ctypes.c_int, [_vp, _fp, _fp]),
     "mgr_level_set_images_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "mgr_level_evaluate": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),

@@ -631,6 +631,28 @@ mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad)
     });
 }
 
+mgr_status mgr_level_set_grid(mgr_level *lvl, const int csize[3])
+{
+    if (!lvl || !csize) return fail(MGR_ERR_ARG, "null argument");
+    return guarded([&] {
+        if (lvl->images_from) throw StateError("mgr_level_set_grid: level shares another level's images");
+        const int D = lvl->d.dim;
+        int cs[3] = {1, 1, 1};
+        bool same = true;
+        for (int k = 0; k < D; ++k) {
+            if (csize[k] <= 3) throw std::invalid_argument("coefficient grid must be larger than 3 per axis");
+            cs[k] = csize[k];
+            same = same && cs[k] == lvl->nc[k];
+        }
+        if (same) return;
+        // the tile follows the new coefficient spacing as at creation
+        for (int k = 0; k < D; ++k) lvl->nc[k] = cs[k];
+        lvl->choose_tile();
+        level_set_grid(lvl, cs, lvl->tile);
+        ck(cudaStreamSynchronize(lvl->stream), "set_grid sync");
+    });
+}
+
 mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z)
 {
     if (!lvl) return fail(MGR_ERR_ARG, "null level");

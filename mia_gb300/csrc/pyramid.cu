@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -221,6 +222,7 @@ int mirror_h(int index, int width)
 
 void ck(cudaError_t e, const char *what)
 {
+    if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 

@@ -14,6 +14,7 @@
 // values are those of the host code.
 #include <algorithm>
 #include <cstring>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -33,6 +34,7 @@ constexpr int RT = 256;
 
 void ck(cudaError_t e, const char *what)
 {
+    if (e == cudaErrorMemoryAllocation) throw std::bad_alloc();
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 

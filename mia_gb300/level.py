@@ -97,6 +97,16 @@ class Level:
     def _params(self, params):
         return _sized(_d(params), self.nparams, "params")
 
+    def set_grid(self, csize):
+        """a new coefficient grid (x, y[, z]) on the same images"""
+        cs = (ctypes.c_int * 3)(*(list(csize) + [1] * (3 - len(csize))))
+        check(lib().mgr_level_set_grid(self.h, cs))
+        n = ctypes.c_size_t()
+        out = (ctypes.c_int * 3)()
+        check(lib().mgr_level_csize(self.h, out, ctypes.byref(n)))
+        self.csize = tuple(out[: self.dim])
+        self.nparams = n.value
+
     def set_path(self, path="split", tile=(0, 0, 0)):
         p = _lib.PATH_PLAIN if path == "plain" else _lib.PATH_SPLIT
         t = list(tile) + [0] * (3 - len(tile))

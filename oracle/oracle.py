@@ -395,8 +395,9 @@ def minimize_test_problem(mz, x0=(5.0, 7.0)):
 
 
 def register(src, ref, rate, levels, mz, cost="ssd", penalty_weight=None, div=1.0, curl=1.0, ssd_norm=False,
-             cost_weight=1.0, penalty_norm=False, threads=1):
-    """TNonrigidRegisterImpl::run: returns (params, csize, final_cost, evaluations)"""
+             cost_weight=1.0, penalty_norm=False, threads=1, precision=PREC_REF):
+    """TNonrigidRegisterImpl::run: returns (params, csize, final_cost, evaluations);
+    `precision` PREC_F64 runs every evaluation in double"""
     s, r = _f(src), _f(ref)
     d = LevelDesc()
     d.dim = s.ndim
@@ -409,7 +410,7 @@ def register(src, ref, rate, levels, mz, cost="ssd", penalty_weight=None, div=1.
     d.has_penalty = int(penalty_weight is not None)
     d.pen_weight = penalty_weight or 0.0
     d.pen_div, d.pen_curl, d.pen_norm = div, curl, int(penalty_norm)
-    d.precision, d.threads = PREC_REF, threads
+    d.precision, d.threads = precision, threads
     maxp = 1 << 24
     out = np.empty(maxp)
     cs = (ctypes.c_int * 3)()

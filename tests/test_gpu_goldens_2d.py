@@ -86,7 +86,10 @@ def test_golden_c_rate_grid_2d(goldens):
     assert list(lv.csize) == g["coeff_size"]
     img = np.random.default_rng(3).normal(size=tuple(g["size"][::-1])).astype(np.float32)
     lv.set_images(img, img)
-    np.testing.assert_array_equal(lv.warp(np.zeros(lv.nparams)), img)
+    # zero coefficients: the identity; the warp interpolates the image at
+    # the pixel centres, equal to it up to the prefilter's float rounding
+    w = lv.warp(np.zeros(lv.nparams))
+    assert np.max(np.abs(w - img)) <= 1e-5 * np.max(np.abs(img))
 
 
 def _gpu_penalty(size, csize, coeffs, wd, wr, weight=1.0):
@@ -106,6 +109,9 @@ def test_golden_divcurl_matrix_2d_through_gpu(goldens):
         coeffs, fr = golden2d.ppmatrix_coefficients(c)
         size = tuple(int(v) for v in fr)
         csize = (coeffs.shape[1], coeffs.shape[0])
+        # the scale of the terms a near-zero value cancels out of: the full
+        # divcurl value of the same field (float arithmetic on the GPU)
+        scale = abs(O.divcurl_matrix(coeffs, fr, 1.0, 1.0, with_grad=False, as_float=True, mode=1))
         for chk in c["checks"]:
             if chk["wdiv"] == 0.0 and chk["wrot"] == 0.0:
                 continue
@@ -113,7 +119,7 @@ def test_golden_divcurl_matrix_2d_through_gpu(goldens):
             # curl weight is expressed by the div / curl factors
             v = _gpu_penalty(size, csize, coeffs, chk["wdiv"], chk["wrot"])
             o = O.divcurl_matrix(coeffs, fr, chk["wdiv"], chk["wrot"], with_grad=False, as_float=True, mode=1)
-            assert abs(v - o) <= 1e-5 * max(abs(o), 1e-3), (name, chk, v, o)
+            assert abs(v - o) <= 1e-5 * max(abs(o), scale), (name, chk, v, o)
             if chk["expect"] == "zero":
                 assert close_pct(1.0 + v, 1.0, chk["tol_pct"]), (name, chk, v)
             else:
