@@ -172,6 +172,27 @@ def split_vs_plain(lv, p_d, g_d, c_d, flush, steps, N):
             "speedup_split_vs_plain": t_plain / t_split}
 
 
+def fused_vs_split(lv, p_d, g_d, c_d, flush, steps, N, params, tz=16):
+    """the fused SSD kernel (warp, force and adjoint in one pass per tile,
+    MGR_PATH_FUSED) against the split kernels, same GPU, same inputs: device
+    ms per evaluation and the fused result's difference from the split one"""
+    t_split = time_evals(lv, p_d, g_d, c_d, flush, steps)
+    k_split = lv.kernel_times()
+    ref = lv.evaluate(params)
+    lv.set_path("fused", (0, 0, tz))
+    t_fused = time_evals(lv, p_d, g_d, c_d, flush, steps)
+    k_fused = lv.kernel_times()
+    got = lv.evaluate(params)
+    lv.set_path("split")
+    return {"split_ms": t_split, "fused_ms": t_fused, "speedup_fused_vs_split": t_split / t_fused,
+            "fused_value": N / t_fused / 1e3, "unit": "Mvoxel/s", "fused_tile": [30, 8, tz],
+            "kernel_ms_split": {"warp": k_split[0], "adjoint": k_split[1], "gather_penalty": k_split[2]},
+            "kernel_ms_fused": {"fused": k_fused[0], "gather_penalty": k_fused[2]},
+            "fused_vs_split_cost_rel": abs(got[0] - ref[0]) / abs(ref[0]),
+            "fused_vs_split_grad_rel_l2": float(np.linalg.norm(got[2] - ref[2]) / np.linalg.norm(ref[2])),
+            "kept": "split" if t_split <= t_fused else "fused"}
+
+
 def fd_check(w, mov, ref, params, lv, ref_grads, threads, ncoef=64, h=1e-3, seed=7):
     """the gradient against FP64 central finite differences of the FP64
     oracle's total cost on `ncoef` random coefficients; the reference's own
@@ -624,6 +645,9 @@ def run_gpu(args):
     }
     if ws == 1:
         line["split_vs_plain"] = split_vs_plain(lv, p_d, g_d, c_d, flush, max(3, min(args.steps, 10)), N)
+        if w["cost"] == "ssd":
+            line["fused_vs_split"] = fused_vs_split(lv, p_d, g_d, c_d, flush, max(3, min(args.steps, 10)), N,
+                                                    params)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, n, dt, res = cpu_baseline(w, mov, ref, params, args.cpu_seconds, threads)

@@ -43,8 +43,13 @@ enum { MGR_COST_SSD = 0, MGR_COST_NCC = 1 };
                    per-coefficient gather (default, fastest).
    MGR_PATH_PLAIN: one kernel per reference step (dense grid, warp, image
                    gradient, force, separable translate, value) — the plain
-                   per-pair drop-in used as the comparison baseline. */
-enum { MGR_PATH_SPLIT = 0, MGR_PATH_PLAIN = 1 };
+                   per-pair drop-in used as the comparison baseline.
+   MGR_PATH_FUSED: 3D SSD only: one kernel computes, per tile, the warped
+                   image with a one-voxel halo, the force and its adjoint
+                   contraction (the warped image is neither stored nor read
+                   back), then the per-coefficient gather.  The value-only
+                   entry points of such a level run the split path's warp. */
+enum { MGR_PATH_SPLIT = 0, MGR_PATH_PLAIN = 1, MGR_PATH_FUSED = 2 };
 
 /* Level description; field names follow the plugin parameters:
    spline:rate, image:cost/weight, ssd:norm, divcurl:weight/div/curl/norm. */

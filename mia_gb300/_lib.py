@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libmgr.so")
 
 MGR_OK, MGR_ERR_ARG, MGR_ERR_CUDA, MGR_ERR_OOM, MGR_ERR_TIMEOUT, MGR_ERR_STATE = range(6)
 COST_SSD, COST_NCC = 0, 1
-PATH_SPLIT, PATH_PLAIN = 0, 1
+PATH_SPLIT, PATH_PLAIN, PATH_FUSED = 0, 1, 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)

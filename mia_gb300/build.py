@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libmgr.so")
 BUILD = os.path.join(HERE, "_build")
 
-CU_SOURCES = ["api.cu", "eval.cu", "split.cu", "split3.cu", "gather.cu", "prefilter.cu", "noalloc.cu", "pyramid.cu", "register.cu", "batch.cu", "refine.cu"]
+CU_SOURCES = ["api.cu", "eval.cu", "split.cu", "split3.cu", "fused3.cu", "gather.cu", "prefilter.cu", "noalloc.cu", "pyramid.cu", "register.cu", "batch.cu", "refine.cu"]
 CXX_SOURCES = ["tables.cc", "driver.cc", "tune.cc", "transio.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 TILES_JSON = os.path.join(HERE, "tiles.json")

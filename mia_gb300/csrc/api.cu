@@ -441,6 +441,23 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         return;
     }
     L->ev_recorded = L->timing;
+    if (L->path == MGR_PATH_FUSED) {
+        // the fused kernel and the gather on the fused tiles' tables; the
+        // call's buffers as the caller set them in a
+        EvalArgs af = L->args(true);
+        af.params = a.params;
+        af.grad_total = a.grad_total;
+        af.grad_image = a.grad_image;
+        af.grad_penalty = a.grad_penalty;
+        af.costs = a.costs;
+        L->record(0);
+        launch_fused3(af, 1, st);
+        L->record(1);
+        L->record(2);
+        launch_gather(af, 1, st);
+        L->record(3);
+        return;
+    }
     if (L->path == MGR_PATH_PLAIN) {
         L->record(0);
         const size_t tsz = size_t(std::max(L->nc[2], 1)) * std::max(L->n[1], L->nc[1]) * L->n[0] * 3;
@@ -656,9 +673,19 @@ mgr_status mgr_level_set_grid(mgr_level *lvl, const int csize[3])
 mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z)
 {
     if (!lvl) return fail(MGR_ERR_ARG, "null level");
-    if (path != MGR_PATH_SPLIT && path != MGR_PATH_PLAIN) return fail(MGR_ERR_ARG, "unknown path");
+    if (path != MGR_PATH_SPLIT && path != MGR_PATH_PLAIN && path != MGR_PATH_FUSED)
+        return fail(MGR_ERR_ARG, "unknown path");
     return guarded([&] {
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        if (path == MGR_PATH_FUSED) {
+            if (lvl->d.dim != 3 || lvl->d.cost != MGR_COST_SSD)
+                throw std::invalid_argument("the fused path evaluates 3D SSD only");
+            if (lvl->images_from) throw StateError("the fused path needs the level's own images");
+            for (int k = 0; k < 3; ++k)
+                if (lvl->nc[k] - 3 > lvl->n[k] - 1)
+                    throw std::invalid_argument("the fused path needs a coefficient spacing of at least one voxel");
+        }
+        const bool fused_change = (path == MGR_PATH_FUSED) != (lvl->path == MGR_PATH_FUSED);
         lvl->path = path;
         int t[3] = {tile_x > 0 ? tile_x : lvl->tile[0], tile_y > 0 ? tile_y : lvl->tile[1],
                     tile_z > 0 ? tile_z : lvl->tile[2]};
@@ -666,7 +693,7 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
         if (!tile_supported(lvl->d.dim, t[0], t[1], t[2]))
             throw std::invalid_argument("tile shape not compiled in (3D: 32x8x32, 32x8x16, 32x8x8, 32x8x4; "
                                         "2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
-        bool changed = false;
+        bool changed = fused_change;
         for (int k = 0; k < 3; ++k)
             if (t[k] != lvl->tile[k]) {
                 lvl->tile[k] = t[k];
@@ -676,6 +703,10 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
             ck(cudaStreamSynchronize(lvl->stream), "sync");
             lvl->build_tables();
             ck(cudaStreamSynchronize(lvl->stream), "sync");
+        }
+        if (path == MGR_PATH_FUSED && fused3_smem(lvl->args(true)) > size_t(227) * 1024) {
+            lvl->path = MGR_PATH_SPLIT;
+            throw std::invalid_argument("the fused kernel's shared memory does not fit at this coefficient spacing");
         }
     });
 }

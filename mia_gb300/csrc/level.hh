@@ -142,6 +142,11 @@ struct mgr_level {
     int tile[3] = {32, 8, 16};
     AxisDev ax[3];
     DevBuf<unsigned char> axis_tables;   // the packed AxisDev tables
+    // MGR_PATH_FUSED: the tables of the fused kernel's tiles (30 x 8 x TZ),
+    // for its launch and the gather after it; the other kernels keep ax
+    AxisDev axf[3];
+    DevBuf<unsigned char> axis_tables_f;
+    int slot_f = 0;
     DevBuf<float> coef, coef_pad, ref, warped, minmax, partial, ptable, pen_val, params_f;
     DevBuf<float2> mmpart;
     DevBuf<double> params, grad_total, grad_image, grad_penalty, scalars, costs, tile_sums, pen_part, means, mpart;
@@ -168,6 +173,7 @@ struct mgr_level {
             if (b.p) b.st = s;
         };
         re(axis_tables);
+        re(axis_tables_f);
         re(coef), re(coef_pad), re(ref), re(warped), re(minmax), re(partial), re(ptable), re(pen_val), re(params_f);
         re(mmpart);
         re(params), re(grad_total), re(grad_image), re(grad_penalty), re(scalars), re(costs), re(tile_sums);
@@ -200,7 +206,8 @@ struct mgr_level {
     // outlives this one; only one of the two is evaluated at a time
     const mgr_level *images_from = nullptr;
 
-    EvalArgs args() const
+    // the kernels' arguments; `fused`: with the fused kernel's tile tables
+    EvalArgs args(bool fused = false) const
     {
         const mgr_level &I = images_from ? *images_from : *this;
         EvalArgs a{};
@@ -210,7 +217,7 @@ struct mgr_level {
         for (int k = 0; k < 3; ++k) {
             a.n[k] = n[k];
             a.nc[k] = nc[k];
-            a.ax[k] = ax[k].view();
+            a.ax[k] = fused ? axf[k].view() : ax[k].view();
         }
         a.coef_img = I.coef.p;
         a.coef_pad = I.coef_pad.p;
@@ -225,7 +232,7 @@ struct mgr_level {
         a.cost_weight = d.cost_weight;
         a.centers = I.means.p;
         a.partial = partial.p;
-        a.slot = slot;
+        a.slot = fused ? slot_f : slot;
         a.tile_sums = tile_sums.p;
         a.counters = counters.p;
         a.scalars = scalars.p;
@@ -289,11 +296,14 @@ struct mgr_level {
         }
     }
 
-    void build_tables()
+    // the per-axis tables of tiles t into A (packed, uploaded to tables);
+    // returns the number of tiles and sets the partial slot size
+    int build_axis_set(const int t[3], AxisDev (&A)[3], DevBuf<unsigned char> &tables, int &slot_size)
     {
         const int D = d.dim;
+        AxisDev *ax = A;
         std::vector<unsigned char> blob;
-        for (int k = 0; k < D; ++k) build_axis(ax[k].h, n[k], nc[k], tile[k]);
+        for (int k = 0; k < D; ++k) build_axis(ax[k].h, n[k], nc[k], t[k]);
         if (D == 3) {
             // per axis and coefficient: the partial-slot offset parts of the
             // tiles that hold it, slot entry (tx, ty, tz) of coefficient
@@ -319,14 +329,36 @@ struct mgr_level {
         }
         for (int k = 0; k < D; ++k) ax[k].pack_all(blob);
         // a fresh buffer: kernels queued earlier may still read the old one
-        axis_tables.release();
-        axis_tables.upload(blob, stream);
-        for (int k = 0; k < D; ++k) ax[k].base = axis_tables.p;
-        const int ntiles = ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
-        slot = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
-        partial.alloc(size_t(ntiles) * slot, stream);
+        tables.release();
+        tables.upload(blob, stream);
+        for (int k = 0; k < D; ++k) ax[k].base = tables.p;
+        slot_size = D * ax[0].h.ac * ax[1].h.ac * (D == 3 ? ax[2].h.ac : 1);
+        return ax[0].h.nt * ax[1].h.nt * (D == 3 ? ax[2].h.nt : 1);
+    }
+
+    // the fused kernel's tile: 30 interior voxels in x (32 lanes with the
+    // halo), 8 rows, the level's z tile
+    void fused_tile(int t[3]) const
+    {
+        t[0] = 30;
+        t[1] = 8;
+        t[2] = tile[2];
+    }
+
+    void build_tables()
+    {
+        const int ntiles = build_axis_set(tile, ax, axis_tables, slot);
+        size_t part = size_t(ntiles) * slot, sums = size_t(ntiles);
+        if (path == MGR_PATH_FUSED) {
+            int t[3];
+            fused_tile(t);
+            const int ntf = build_axis_set(t, axf, axis_tables_f, slot_f);
+            part = std::max(part, size_t(ntf) * slot_f);
+            sums = std::max(sums, size_t(ntf));
+        }
+        partial.alloc(part, stream);
         const size_t plain_blocks = (N + 255) / 256;
-        tile_sums.alloc(std::max<size_t>(ntiles, plain_blocks) * 5, stream);
+        tile_sums.alloc(std::max<size_t>(sums, plain_blocks) * 5, stream);
         pen_part.alloc(size_t(gather_blocks(args())) + 1, stream);
         tables_valid = true;
     }

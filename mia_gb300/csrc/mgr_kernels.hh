@@ -112,6 +112,11 @@ bool tile_supported3(int tx, int ty, int tz);
 size_t split3_smem(const EvalArgs &a, int which);
 void launch_warp3(const EvalArgs &a, cudaStream_t st);
 void launch_adjoint3(const EvalArgs &a, cudaStream_t st);
+// the fused SSD kernel (fused3.cu): warp, force and adjoint in one pass per
+// 30 x 8 x TZ tile; with_gradient = 0 sums the cost only
+bool tile_supported_fused3(int tx, int ty, int tz);
+size_t fused3_smem(const EvalArgs &a);
+void launch_fused3(const EvalArgs &a, int with_gradient, cudaStream_t st);
 int gather3_blocks(const EvalArgs &a);
 void launch_gather3(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st);
 void prepare_split3_batch(int tz, size_t sm_warp, size_t sm_adj);

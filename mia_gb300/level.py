@@ -108,7 +108,7 @@ class Level:
         self.nparams = n.value
 
     def set_path(self, path="split", tile=(0, 0, 0)):
-        p = _lib.PATH_PLAIN if path == "plain" else _lib.PATH_SPLIT
+        p = {"plain": _lib.PATH_PLAIN, "fused": _lib.PATH_FUSED}.get(path, _lib.PATH_SPLIT)
         t = list(tile) + [0] * (3 - len(tile))
         check(lib().mgr_level_set_path(self.h, p, *t))
 
