@@ -20,6 +20,7 @@
 #include <array>
 #include <atomic>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -700,6 +701,23 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         std::vector<const float *> in_src(npairs), in_ref(npairs);
         std::vector<float *> out_src(npairs), out_ref(npairs);
         std::vector<size_t> nvox(npairs);
+        // host images on a device that reads pageable host memory
+        // coherently (address translation through the host's page tables,
+        // as on Grace-based systems): the normalisation kernels read the
+        // caller's arrays where they are, with no staged copy (the host path
+        // then costs two reads of the images over the CPU-GPU link);
+        // MGR_HOST_COPY=1 keeps the copies
+        bool direct = false;
+        if (!images_on_device) {
+            int pageable = 0, host_tables = 0;
+            const char *force_copy = std::getenv("MGR_HOST_COPY");
+            if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
+                cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) ==
+                    cudaSuccess)
+                direct = pageable == 1 && host_tables == 1 && !(force_copy && *force_copy && *force_copy != '0');
+            cudaGetLastError();
+        }
+        trace_count("batch: images read in place (1 = yes)", direct ? 1.0 : 0.0);
         for (int p = 0; p < npairs; ++p) {
             std::unique_ptr<PairRun> r(new PairRun);
             r->full = descs[p];
@@ -708,7 +726,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             r->ref_n.alloc(n, st);
             in_src[p] = srcs[p];
             in_ref[p] = refs[p];
-            if (!images_on_device) {
+            if (!images_on_device && !direct) {
                 r->src.alloc(n, st);
                 r->ref.alloc(n, st);
                 in_src[p] = r->src.p;
@@ -719,7 +737,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
             nvox[p] = n;
             pairs.push_back(std::move(r));
         }
-        if (!images_on_device) {
+        if (!images_on_device && !direct) {
             // host images: the copies from pageable memory are staged by the
             // calling thread, so the pairs are uploaded from several host
             // threads, each on its own per-thread stream

@@ -189,6 +189,17 @@ def test_batch_from_device_images_equals_host_images_and_matches_oracle():
     for (ph, ch, fh, nh), (pd, cd, fd, nd) in zip(host, dev):
         assert ch == cd and fh == fd and nh == nd
         assert np.array_equal(ph, pd)
+    # host arrays read in place by the device (where it can read pageable
+    # host memory) and host arrays staged by copies give the same bits
+    import os
+    os.environ["MGR_HOST_COPY"] = "1"
+    try:
+        copied = R.register_batch(pairs, 8.0, 3, mg, **kw)
+    finally:
+        del os.environ["MGR_HOST_COPY"]
+    for (ph, ch, fh, nh), (pc, cc, fc, nc) in zip(host, copied):
+        assert ch == cc and fh == fc and nh == nc
+        assert np.array_equal(ph, pc)
     mo = O.minimizer("gsl", maxiter=5, step=0.1)
     for (mov, ref), (pg, csg, fg, ng) in zip(pairs, host):
         po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, 8.0, 3, mo, **kw)
