@@ -451,10 +451,16 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         af.grad_penalty = a.grad_penalty;
         af.costs = a.costs;
         L->record(0);
-        launch_fused3(af, 1, st);
+        {
+            NvtxRange r("k_fused3");
+            launch_fused3(af, 1, st);
+        }
         L->record(1);
         L->record(2);
-        launch_gather(af, 1, st);
+        {
+            NvtxRange r("k_gather3");
+            launch_gather(af, 1, st);
+        }
         L->record(3);
         return;
     }
@@ -474,11 +480,20 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         return;
     }
     L->record(0);
-    launch_warp(a, st);
+    {
+        NvtxRange r(L->d.dim == 3 ? "k_warp3" : "k_warp (2D)");
+        launch_warp(a, st);
+    }
     L->record(1);
-    launch_adjoint(a, st);
+    {
+        NvtxRange r(L->d.dim == 3 ? "k_adjoint3" : "k_adjoint (2D)");
+        launch_adjoint(a, st);
+    }
     L->record(2);
-    launch_gather(a, 1, st);
+    {
+        NvtxRange r(L->d.dim == 3 ? "k_gather3" : "k_gather (2D)");
+        launch_gather(a, 1, st);
+    }
     L->record(3);
 }
 
@@ -486,6 +501,7 @@ extern "C" {
 
 mgr_status mgr_level_set_images(mgr_level *lvl, const float *src, const float *ref)
 {
+    NvtxRange nvtx_range("mgr_level_set_images");
     if (!lvl || !src || !ref) return fail(MGR_ERR_ARG, "null argument");
     return guarded([&] {
         for (size_t i = 0; i < lvl->N; ++i)
@@ -507,6 +523,7 @@ mgr_status mgr_level_set_images_device(mgr_level *lvl, const float *d_src, const
 
 mgr_status mgr_level_evaluate_device(mgr_level *lvl, const double *d_params, double *d_grad_total, double *d_costs)
 {
+    NvtxRange nvtx_range("mgr_level_evaluate_device");
     if (!lvl || !d_params || !d_grad_total) return fail(MGR_ERR_ARG, "null argument");
     return guarded([&] {
         if (!lvl->images_set) throw StateError("set_images must be called before evaluate");
@@ -523,6 +540,7 @@ mgr_status mgr_level_evaluate_device(mgr_level *lvl, const double *d_params, dou
 mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad_total, double *grad_image,
                               double *grad_penalty, double *cost_image, double *cost_penalty)
 {
+    NvtxRange nvtx_range("mgr_level_evaluate");
     if (!lvl || !params) return fail(MGR_ERR_ARG, "null argument");
     return guarded([&] {
         if (!lvl->images_set) throw StateError("set_images must be called before evaluate");
@@ -561,6 +579,7 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
 
 mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_image, double *cost_penalty)
 {
+    NvtxRange nvtx_range("mgr_level_value");
     if (!lvl || !params) return fail(MGR_ERR_ARG, "null argument");
     return guarded([&] {
         if (!lvl->images_set) throw StateError("set_images must be called before value");
