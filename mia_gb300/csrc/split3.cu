@@ -16,10 +16,10 @@
 //       planes in shared memory that bulk copies fill ahead of the walk from
 //       a mirror-padded copy (the box of a plane follows from the range of
 //       u over the tile), so the interior needs no index folding and the
-//       gather costs shared-memory wavefronts instead of L1 lines; the
-//       warped image is written and
-//       the SSD / NCC sums are accumulated; the last block finalises the
-//       cost.
+//       gather costs shared-memory wavefronts instead of L1 lines; each
+//       thread samples two planes per step (two independent tap chains in
+//       flight); the warped image is written and the SSD / NCC sums are
+//       accumulated; the last block finalises the cost.
 //   k_adjoint3<TZ>    central differences of the warped image (x neighbours
 //       by warp shuffle, y neighbours from the rows of the adjacent warps, z
 //       neighbours carried in registers; mia/3d/image.cc:347-466), the SSD /
@@ -319,67 +319,42 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     int kwait = 0;      // planes below kwait have arrived
     // the reference is streamed three planes ahead of its use (registers
     // r0..r2), so the walk does not wait on its memory latency
-    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    // two planes per step: the two voxels' tap gathers are independent
+    // chains, so a warp keeps twice the loads in flight; the waits, the
+    // displacement window and the refills are done per pair.  Per voxel the
+    // arithmetic and the order of the sums are those of one plane per step.
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, r3 = 0.0f;
     if (inxy) {
         r0 = __ldg(rin);
         if (ez > 1) r1 = __ldg(rin + nxy);
         if (ez > 2) r2 = __ldg(rin + 2 * nxy);
+        if (ez > 3) r3 = __ldg(rin + 3 * nxy);
     }
-    for (int t = 0; t < ez; ++t) {
-        advance(t);
-        if (ring_ok) {
-            // the planes of this step (t .. t + span - 1) must have arrived;
-            // after any thread of the block gave up, none waits again
-            while (kwait <= t + span - 1) {
-                if (ring_failed || !mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u)) {
-                    if (!ring_failed) {
-                        ring_failed = 1;
-                        atomicOr(&a.counters[6], 1u);
-                    }
-                    ring_ok = false;
-                    break;
-                }
-                ++kwait;
-            }
+    auto sample = [&](int t, const float u[3]) -> float {
+        const int z = z0 + t;
+        const float px = px0 - u[0], py = py0 - u[1], pz = float(z) - u[2];
+        const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
+        const int col = fx - 1 - bxs, row = fy - 1 - bylo, kk = fz - 1 - bzbase;
+        if (ring_ok && unsigned(col) < unsigned(bw4 - 3) && unsigned(row) < unsigned(brows - 3) &&
+            unsigned(kk - t) < unsigned(span - 3))
+            return taps3_ring(ring, ring_slot(kk), row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
+        return taps3_global(a, px, py, pz, mn, mxv);
+    };
+    auto add_cost = [&](float wv, float b) {
+        if (a.cost == 0) {
+            const float d = wv - b;
+            acc[0] += d * d;
+        } else {
+            const float da = wv - ca, db = b - cb;
+            acc[0] += da;
+            acc[1] += db;
+            acc[2] += da * da;
+            acc[3] += db * db;
+            acc[4] += da * db;
         }
-        const float4 wz = zw[t];
-        float u[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) u[c] = wz.x * q[c][0] + wz.y * q[c][1] + wz.z * q[c][2] + wz.w * q[c][3];
-        if (inxy) {
-            const int z = z0 + t;
-            const float px = px0 - u[0], py = py0 - u[1], pz = float(z) - u[2];
-            const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
-            const int col = fx - 1 - bxs, row = fy - 1 - bylo, kk = fz - 1 - bzbase;
-            float wv;
-            if (ring_ok && col >= 0 && col + 3 < bw4 && row >= 0 && row + 3 < brows && kk >= t && kk + 3 <= t + span - 1)
-                wv = taps3_ring(ring, ring_slot(kk), row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
-            else
-                wv = taps3_global(a, px, py, pz, mn, mxv);
-            *wout = wv;
-            const float b = r0;
-            if (a.cost == 0) {
-                const float d = wv - b;
-                acc[0] += d * d;
-            } else {
-                const float da = wv - ca, db = b - cb;
-                acc[0] += da;
-                acc[1] += db;
-                acc[2] += da * da;
-                acc[3] += db * db;
-                acc[4] += da * db;
-            }
-        }
-        r0 = r1;
-        r1 = r2;
-        r2 = (inxy && t + 3 < ez) ? __ldg(rin + 3 * nxy) : 0.0f;
-        wout += nxy;
-        rin += nxy;
+    };
+    auto release = [&](int t) {   // this warp is done with plane t
         if (staged && t + RING_N < nplanes) {
-            // this warp is done with plane t; the last warp to be done
-            // refills the slot with plane t + RING_N (the warps run apart
-            // by up to the ring's slack instead of meeting at a barrier
-            // every plane)
             __syncwarp();
             if (lane == 0) {
                 const int slot = ring_slot(t);
@@ -394,6 +369,55 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
                 }
             }
         }
+    };
+    for (int t = 0; t < ez; t += 2) {
+        const bool two = t + 1 < ez;
+        float ua[3], ub[3] = {0.0f, 0.0f, 0.0f};
+        advance(t);
+        {
+            const float4 wz = zw[t];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ua[c] = wz.x * q[c][0] + wz.y * q[c][1] + wz.z * q[c][2] + wz.w * q[c][3];
+        }
+        if (two) {
+            advance(t + 1);
+            const float4 wz = zw[t + 1];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ub[c] = wz.x * q[c][0] + wz.y * q[c][1] + wz.z * q[c][2] + wz.w * q[c][3];
+        }
+        if (ring_ok) {
+            const int need = t + span - (two ? 0 : 1);
+            while (kwait <= need) {
+                if (!mbar_wait(smem_u32(&mbar[ring_slot(kwait)]), unsigned(kwait / RING_N) & 1u) || ring_failed) {
+                    if (!ring_failed) {
+                        ring_failed = 1;
+                        atomicOr(&a.counters[6], 1u);
+                    }
+                    ring_ok = false;
+                    break;
+                }
+                ++kwait;
+            }
+        }
+        if (inxy) {
+            const float wa = sample(t, ua);
+            float wb = 0.0f;
+            if (two) wb = sample(t + 1, ub);
+            wout[0] = wa;
+            add_cost(wa, r0);
+            if (two) {
+                wout[nxy] = wb;
+                add_cost(wb, r1);
+            }
+        }
+        r0 = r2;
+        r1 = r3;
+        r2 = (inxy && t + 4 < ez) ? __ldg(rin + 4 * nxy) : 0.0f;
+        r3 = (inxy && t + 5 < ez) ? __ldg(rin + 5 * nxy) : 0.0f;
+        wout += 2 * nxy;
+        rin += 2 * nxy;
+        release(t);
+        if (two) release(t + 1);
     }
     if (staged) __syncthreads();   // every warp is done with the ring
     if (staged && tid == 0) {
