@@ -245,8 +245,12 @@ mgr_status mgr_register(const mgr_level_desc *desc, int levels, const mgr_minimi
    dimension, cost and penalty; sizes may differ.  Each pair follows the same
    levels / refine / minimizer sequence as mgr_register, but the minimizers
    run as device state machines and one step evaluates every unfinished
-   pair with one launch per kernel over a (pair, tile) work list; with
-   `use_graphs` the steps of each level are captured as a CUDA graph.
+   pair with one launch per kernel over a (pair, tile) work list.
+   `use_graphs` is a set of flags: 1, the steps of each level are captured
+   as a CUDA graph; 2 (3D), the warp and adjoint kernels run as persistent
+   launches — as many blocks as stay resident, drawing (pair, tile) items
+   from a device queue — instead of one block per item (same results bit
+   for bit).
    csize_out holds 3 ints per pair; params_out[p] receives max_params[p]
    doubles at most (sized as for mgr_register). */
 mgr_status mgr_register_batch(int npairs, const mgr_level_desc *descs, int levels,

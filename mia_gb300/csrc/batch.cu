@@ -395,7 +395,7 @@ void ckm(mgr_status s)
 // Run the minimizer of every pair with in_pass set, in lock step, until all
 // have finished.  Steps are captured into a CUDA graph when use_graphs.
 void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_desc &mz, int dim, int tile[3],
-              bool use_graphs, cudaStream_t st, const char *label)
+              bool use_graphs, bool persistent, cudaStream_t st, const char *label)
 {
     std::vector<int> members;
     for (size_t i = 0; i < pairs.size(); ++i)
@@ -457,6 +457,7 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     const size_t o_gitems = place(sizeof(int2) * gitems.size()), o_nblocks = place(sizeof(int) * np);
     const size_t o_active = place(sizeof(int) * np), o_count = place(sizeof(int));
     const size_t o_moved = place(sizeof(int) * np), o_mcount = place(sizeof(unsigned) * np);
+    const size_t o_queue = place(sizeof(int) * 4);   // the persistent kernels' queues (warp, adjoint)
     const size_t o_mpart = place(sizeof(double) * size_t(np) * msc.nblk * 3);
     std::vector<unsigned char> blob(o_mpart, 0);
     std::memcpy(blob.data() + o_args, args.data(), sizeof(EvalArgs) * np);
@@ -476,18 +477,36 @@ void run_pass(std::vector<std::unique_ptr<PairRun>> &pairs, const mgr_minimizer_
     int *d_nblocks = reinterpret_cast<int *>(d_pass.p + o_nblocks);
     int *d_active = reinterpret_cast<int *>(d_pass.p + o_active);
     int *d_count = reinterpret_cast<int *>(d_pass.p + o_count);
+    int *d_queue = reinterpret_cast<int *>(d_pass.p + o_queue);
     msc.part = reinterpret_cast<double *>(d_pass.p + o_mpart);
     msc.count = reinterpret_cast<unsigned *>(d_pass.p + o_mcount);
     msc.moved = reinterpret_cast<int *>(d_pass.p + o_moved);
     const dim3 mgrid(msc.nblk, np);
 
+    // persistent launches (3D): as many blocks as stay resident, drawing
+    // (pair, tile) items from the device queue; the grid sizes are fixed
+    // before any capture
+    const bool queue = persistent && dim == 3;
+    int qgrid[2] = {0, 0};
+    if (queue) {
+        prepare_split_batch(dim, tile[0], tile[1], tile[2], sm_warp, sm_adj);
+        qgrid[0] = std::min(int(titems.size()), split3_queue_grid(tile[2], 0, sm_warp));
+        qgrid[1] = std::min(int(titems.size()), split3_queue_grid(tile[2], 1, sm_adj));
+    }
     auto step = [&]() {
         k_min_propose<<<mgrid, MT, 0, st>>>(d_states, d_vecs, mz, d_active, msc);
-        if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
-                                d_active, sm_warp, 0, st))
-            throw std::invalid_argument("tile shape not compiled in");
-        launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
-                           d_active, sm_adj, 1, st);
+        if (queue) {
+            launch_split3_queue(tile[2], d_args, d_titems, int(titems.size()), d_active, d_queue, qgrid[0], sm_warp,
+                                0, st);
+            launch_split3_queue(tile[2], d_args, d_titems, int(titems.size()), d_active, d_queue + 2, qgrid[1], sm_adj,
+                                1, st);
+        } else {
+            if (!launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
+                                    d_active, sm_warp, 0, st))
+                throw std::invalid_argument("tile shape not compiled in");
+            launch_split_batch(dim, tile[0], tile[1], tile[2], d_args, d_titems, int(titems.size()),
+                               d_active, sm_adj, 1, st);
+        }
         launch_gather_batch(dim, d_args, d_gitems, int(gitems.size()), d_active, d_nblocks, has_pen, st);
         k_min_update<<<mgrid, MT, 0, st>>>(d_states, d_vecs, mz, d_active, msc);
         count_launch(2);
@@ -984,7 +1003,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                 tr_grid.stop();
                 tr_lvl.stop();
                 const std::string label = "level " + std::to_string(shift) + " pass " + std::to_string(pass);
-                run_pass(pairs, *mz, dim, tile, use_graphs != 0, st, label.c_str());
+                run_pass(pairs, *mz, dim, tile, (use_graphs & 1) != 0, (use_graphs & 2) != 0, st, label.c_str());
             }
             for (auto &rp : pairs)
                 for (int k = 0; k < 3; ++k) rp->prev[k] = rp->size[k];

@@ -112,6 +112,12 @@ bool tile_supported3(int tx, int ty, int tz);
 size_t split3_smem(const EvalArgs &a, int which);
 void launch_warp3(const EvalArgs &a, cudaStream_t st);
 void launch_adjoint3(const EvalArgs &a, cudaStream_t st);
+// persistent batched 3D warp (which = 0) and adjoint (1) kernels: `grid`
+// resident blocks draw the items from the device queue queue[0..1] (zero
+// before the first launch; the last block resets it)
+int split3_queue_grid(int tz, int which, size_t sm);
+void launch_split3_queue(int tz, const EvalArgs *args, const int2 *items, int nitems, const int *active, int *queue,
+                         int grid, size_t sm, int which, cudaStream_t st);
 // the fused SSD kernel (fused3.cu): warp, force and adjoint in one pass per
 // 30 x 8 x TZ tile; with_gradient = 0 sums the cost only
 bool tile_supported_fused3(int tx, int ty, int tz);

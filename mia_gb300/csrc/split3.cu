@@ -983,6 +983,68 @@ __global__ void __launch_bounds__(NT3) k_adjoint3_batch(const EvalArgs *__restri
     adjoint3_body<TZ>(a, bx, by, bz, it.y);
 }
 
+// Persistent forms of the batched warp and adjoint kernels: a grid of
+// resident blocks draws (pair, tile) items from a device queue (queue[0],
+// one atomic per item); the last block to finish resets the queue for the
+// next launch (queue[1] counts finished blocks), so the launch can be
+// replayed from a CUDA graph.
+__device__ __forceinline__ bool next_item(int *queue, int nitems, const int2 *items, int2 &it, int &slot)
+{
+    __syncthreads();   // every thread is done with the previous item's shared memory
+    if (threadIdx.x == 0) slot = atomicAdd(&queue[0], 1);
+    __syncthreads();
+    const int i = slot;
+    if (i >= nitems) return false;
+    it = items[i];
+    return true;
+}
+
+__device__ __forceinline__ void queue_done(int *queue)
+{
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&queue[1], 1) == int(gridDim.x) - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3_queue(const EvalArgs *__restrict__ args,
+                                                                    const int2 *__restrict__ items, int nitems,
+                                                                    const int *__restrict__ active, int *queue)
+{
+    __shared__ int slot;
+    int2 it;
+    while (next_item(queue, nitems, items, it, slot)) {
+        if (!active[it.x]) continue;
+        const EvalArgs &a = args[it.x];
+        int bx, by, bz, nt;
+        decode_tile3(a, it.y, bx, by, bz, nt);
+        warp3_body<TZ>(a, bx, by, bz, nt, it.y);
+    }
+    queue_done(queue);
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(NT3) k_adjoint3_queue(const EvalArgs *__restrict__ args,
+                                                        const int2 *__restrict__ items, int nitems,
+                                                        const int *__restrict__ active, int *queue)
+{
+    __shared__ int slot;
+    int2 it;
+    while (next_item(queue, nitems, items, it, slot)) {
+        if (!active[it.x]) continue;
+        const EvalArgs &a = args[it.x];
+        int bx, by, bz, nt;
+        decode_tile3(a, it.y, bx, by, bz, nt);
+        adjoint3_body<TZ>(a, bx, by, bz, it.y);
+    }
+    queue_done(queue);
+}
+
 __global__ void __launch_bounds__(GT3) k_gather3_batch(const EvalArgs *__restrict__ args,
                                                        const int2 *__restrict__ items, const int *__restrict__ active,
                                                        const int *__restrict__ nblocks)
@@ -1055,6 +1117,30 @@ void prepare3_z(size_t sm_warp, size_t sm_adj)
 {
     cudaFuncSetAttribute(k_warp3_batch<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_warp));
     cudaFuncSetAttribute(k_adjoint3_batch<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_adj));
+    cudaFuncSetAttribute(k_warp3_queue<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_warp));
+    cudaFuncSetAttribute(k_adjoint3_queue<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm_adj));
+}
+
+// resident blocks of the persistent kernels (blocks per SM x SMs)
+template <int TZ>
+int queue_grid_z(int which, size_t sm)
+{
+    int per_sm = 0;
+    if (which == 0)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_warp3_queue<TZ>, NT3, sm);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint3_queue<TZ>, NT3, sm);
+    return std::max(1, per_sm) * device_sm_count();
+}
+
+template <int TZ>
+void queue3_z(const EvalArgs *args, const int2 *items, int nitems, const int *active, int *queue, int grid, size_t sm,
+              int which, cudaStream_t st)
+{
+    if (which == 0)
+        k_warp3_queue<TZ><<<grid, NT3, sm, st>>>(args, items, nitems, active, queue);
+    else
+        k_adjoint3_queue<TZ><<<grid, NT3, sm, st>>>(args, items, nitems, active, queue);
 }
 
 }  // namespace
@@ -1113,6 +1199,28 @@ void launch_split3_batch(int tz, const EvalArgs *args, const int2 *items, int ni
     case 8: batch3_z<8>(args, items, nitems, active, sm, which, st); break;
     case 32: batch3_z<32>(args, items, nitems, active, sm, which, st); break;
     default: batch3_z<16>(args, items, nitems, active, sm, which, st); break;
+    }
+    count_launch();
+}
+
+int split3_queue_grid(int tz, int which, size_t sm)
+{
+    switch (tz) {
+    case 4: return queue_grid_z<4>(which, sm);
+    case 8: return queue_grid_z<8>(which, sm);
+    case 32: return queue_grid_z<32>(which, sm);
+    default: return queue_grid_z<16>(which, sm);
+    }
+}
+
+void launch_split3_queue(int tz, const EvalArgs *args, const int2 *items, int nitems, const int *active, int *queue,
+                         int grid, size_t sm, int which, cudaStream_t st)
+{
+    switch (tz) {
+    case 4: queue3_z<4>(args, items, nitems, active, queue, grid, sm, which, st); break;
+    case 8: queue3_z<8>(args, items, nitems, active, queue, grid, sm, which, st); break;
+    case 32: queue3_z<32>(args, items, nitems, active, queue, grid, sm, which, st); break;
+    default: queue3_z<16>(args, items, nitems, active, queue, grid, sm, which, st); break;
     }
     count_launch();
 }

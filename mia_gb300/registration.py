@@ -176,6 +176,8 @@ def normalize_pair(src, ref, device=0):
 
 
 def _batch(shapes, sptrs, rptrs, on_device, rate, levels, mz, device, use_graphs, cost_kw):
+    cost_kw = dict(cost_kw)
+    persistent = cost_kw.pop("persistent", False)   # 3D: persistent warp / adjoint launches
     n = len(shapes)
     descs = (_lib.LevelDesc * n)()
     for i, shp in enumerate(shapes):
@@ -191,7 +193,8 @@ def _batch(shapes, sptrs, rptrs, on_device, rate, levels, mz, device, use_graphs
     fc = (ctypes.c_double * n)()
     ne = (ctypes.c_int * n)()
     fn = lib().mgr_register_batch_device if on_device else lib().mgr_register_batch
-    check(fn(n, descs, int(levels), ctypes.byref(mz), sp, rp, int(device), int(bool(use_graphs)), op, mp, cs, fc, ne))
+    flags = int(bool(use_graphs)) | (2 if persistent else 0)
+    check(fn(n, descs, int(levels), ctypes.byref(mz), sp, rp, int(device), flags, op, mp, cs, fc, ne))
     res = []
     for i, shp in enumerate(shapes):
         dim = len(shp)

@@ -226,3 +226,21 @@ def test_batch_ncc_without_penalty_matches_oracle(dim):
     for (mov, ref), (pg, csg, fg, ng) in zip(pairs, res):
         po, cso, fo, fs, ps = _oracle_with_spread(mov, ref, rate, 2, mo, cost="ncc")
         _assert_close(pg, csg, fg, po, cso, fo, fs, ps)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_batch_persistent_launch_equals_one_block_per_item(use_graphs):
+    """3D NCC, three levels, pairs of uneven size: the persistent warp and
+    adjoint launches (resident blocks drawing (pair, tile) items from a
+    device queue) give bit for bit the results of one block per item"""
+    from mia_gb300 import registration as R
+    shapes = [(40, 44, 48), (48, 40, 36), (40, 36, 44)]
+    pairs = [_pair3d(131 + 5 * i, s) for i, s in enumerate(shapes)]
+    mg = R.minimizer("gsl", maxiter=6, step=0.1)
+    kw = dict(cost="ncc", penalty_weight=5.0)
+    base = R.register_batch(pairs, 8.0, 3, mg, use_graphs=use_graphs, **kw)
+    pers = R.register_batch(pairs, 8.0, 3, mg, use_graphs=use_graphs, persistent=True, **kw)
+    for (pb, cb, fb, nb), (pp, cp, fp, npp) in zip(base, pers):
+        assert cb == cp and fb == fp and nb == npp
+        assert np.array_equal(pb, pp)
