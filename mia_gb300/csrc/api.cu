@@ -417,6 +417,11 @@ static void set_images_impl(mgr_level *L, const float *d_src, const float *d_ref
 
 static void upload_params(mgr_level *L, const double *params)
 {
+    // the copy starts first and the finiteness check runs while it is in
+    // flight; no kernel is queued before the check has passed, and on
+    // failure the copy is waited for (it reads the caller's buffer)
+    ck(cudaMemcpyAsync(L->params.p, params, L->nparams * sizeof(double), cudaMemcpyHostToDevice, L->stream),
+       "params H2D");
     // x - x is 0 for finite x and NaN otherwise: eight independent sums
     // (no branch per value, the loop vectorises) are 0 exactly when every
     // parameter is finite
@@ -428,9 +433,10 @@ static void upload_params(mgr_level *L, const double *params)
     for (; i < n; ++i) acc[0] += params[i] - params[i];
     double all = 0.0;
     for (double v : acc) all += v;
-    if (all != 0.0) throw std::invalid_argument("parameters must be finite");
-    ck(cudaMemcpyAsync(L->params.p, params, L->nparams * sizeof(double), cudaMemcpyHostToDevice, L->stream),
-       "params H2D");
+    if (all != 0.0) {
+        cudaStreamSynchronize(L->stream);
+        throw std::invalid_argument("parameters must be finite");
+    }
 }
 
 static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)

@@ -155,6 +155,32 @@ class Level:
                                        ctypes.byref(ci), ctypes.byref(cp)))
         return ci.value + cp.value, g
 
+    def bind_evaluate_total(self, params, grad_out):
+        """A callable that evaluates at the values `params` holds when it is
+        called, writes the total gradient into `grad_out` and returns the
+        total cost: one mgr_level_evaluate call with the pointers prepared
+        here once (the arrays' contents may change between calls, not the
+        arrays), as a C or C++ caller of the ABI makes it."""
+        for name, a in (("params", params), ("grad_out", grad_out)):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError(name + " must be a C-contiguous float64 array")
+            _sized(a, self.nparams, name)
+        if not grad_out.flags.writeable:
+            raise ValueError("grad_out must be writeable")
+        fn, h = lib().mgr_level_evaluate, self.h
+        pp, gp = params.ctypes.data_as(_dp), grad_out.ctypes.data_as(_dp)
+        ci, cp = ctypes.c_double(), ctypes.c_double()
+        bci, bcp = ctypes.byref(ci), ctypes.byref(cp)
+        keep = (params, grad_out)
+
+        def call():
+            st = fn(h, pp, gp, None, None, bci, bcp)
+            if st:
+                check(st)
+            return ci.value + cp.value
+        call.keep = keep
+        return call
+
     def evaluate_device(self, params_ptr, grad_ptr, costs_ptr):
         check(lib().mgr_level_evaluate_device(self.h, ctypes.c_void_p(params_ptr), ctypes.c_void_p(grad_ptr),
                                               ctypes.c_void_p(costs_ptr)))

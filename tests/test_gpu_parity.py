@@ -459,3 +459,31 @@ def test_bounded_wait_gives_up_and_the_device_stays_usable():
         lv.set_images(mov, ref)
     from mia_gb300 import synth
     check_eval(g, o, o64, synth.smooth_params(g.csize, 1.0, seed=5))
+
+
+def test_bound_evaluate_call_equals_evaluate_total():
+    """the bound C-ABI call (pointers prepared once, the buffers' contents
+    changed between calls) gives evaluate_total's cost and gradient, refuses
+    non-finite parameters, and the level keeps working"""
+    import mia_gb300 as M
+    from mia_gb300 import _lib
+    from mia_gb300 import synth
+    size = (33, 29, 21)
+    lv = M.Level(size, rate=5.0, cost="ssd", penalty_weight=3.0)
+    a, b = make_pair(size[::-1], 5)
+    lv.set_images(a, b)
+    params = np.zeros(lv.nparams)
+    grad = np.zeros(lv.nparams)
+    call = lv.bind_evaluate_total(params, grad)
+    for seed in (1, 2):
+        params[:] = synth.smooth_params(lv.csize, 1.0, seed=seed)
+        c = call()
+        want_c, want_g = lv.evaluate_total(params.copy())
+        assert c == want_c
+        assert np.array_equal(grad, want_g)
+    params[3] = np.nan
+    with pytest.raises(_lib.MgrError) as e:
+        call()
+    assert e.value.status == _lib.MGR_ERR_ARG
+    params[3] = 0.0
+    assert np.isfinite(call())
