@@ -570,6 +570,23 @@ def run_reference_batch(args):
     return 0
 
 
+def e2e_seconds(lv, hp, hg, flush, args):
+    """mean seconds of one evaluation through the C ABI from the host
+    buffers hp (parameters) and hg (gradient), the L2 flushed before each"""
+    import torch
+    evaluate = lv.bind_evaluate_total(hp, hg)   # one C-ABI call per evaluation, pointers prepared once
+    for _ in range(max(1, args.warmup)):
+        evaluate()
+    t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        evaluate()
+        t.append(time.perf_counter() - t0)
+    return float(np.mean(t))
+
+
 def run_gpu(args):
     import torch
     from mia_gb300 import replicas
@@ -614,21 +631,25 @@ def run_gpu(args):
     per = np.array(per)
     value, t_step = replicas.whole_job_rate(N / 1e6, per[:, 3].mean() / 1e3, ws, device=dev)
 
-    # end to end through the C ABI: host (pinned) params in, gradient out
+    # end to end through the C ABI: host (pinned) params in, gradient out;
+    # on a host whose memory the device reads coherently the kernels move
+    # them in place, and a second level with staged copies (MGR_HOST_COPY=1)
+    # is timed beside it
     hp = torch.from_numpy(params).pin_memory().numpy()
     hg = torch.empty(nparams, dtype=torch.float64).pin_memory().numpy()
     lv.set_timing(False)
-    evaluate = lv.bind_evaluate_total(hp, hg)   # one C-ABI call per evaluation, pointers prepared once
-    for _ in range(max(1, args.warmup)):
-        evaluate()
-    e2e_t = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        evaluate()
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_step = replicas.max_over_ranks(float(np.mean(e2e_t)), device=dev)
+    e2e_step = replicas.max_over_ranks(e2e_seconds(lv, hp, hg, flush, args), device=dev)
+    in_place = lv.in_place
+    staged_step = None
+    if in_place:
+        os.environ["MGR_HOST_COPY"] = "1"
+        try:
+            lv_staged = M.Level(size, rate=w["rate"], cost=w["cost"], penalty_weight=w["penalty"], device=local)
+        finally:
+            del os.environ["MGR_HOST_COPY"]
+        lv_staged.set_images(mov, ref)
+        staged_step = replicas.max_over_ranks(e2e_seconds(lv_staged, hp, hg, flush, args), device=dev)
+        del lv_staged
 
     if rank != 0:
         return 0
@@ -655,7 +676,11 @@ def run_gpu(args):
         "config": WL.line_config(name, lv.csize),
         "setup": {"path": "split", "tile": list(lv.tile), "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": ws * N / e2e_step / 1e6, "unit": "Mvoxel/s", "h2d_bytes_per_step": nparams * 8,
-                "d2h_bytes_per_step": nparams * 8 + 16},
+                "d2h_bytes_per_step": nparams * 8 + 16,
+                "transfer": ("in place: the kernels read the parameters and write the gradient and costs in "
+                             "host memory over the coherent CPU-GPU link" if in_place else
+                             "staged: cudaMemcpyAsync of the parameters in, the gradient and costs out"),
+                "staged_value": None if staged_step is None else ws * N / staged_step / 1e6},
         "gpu_launches": int(launches),
         "kernel_ms": {"warp": kms["k_warp3"], "adjoint": kms["k_adjoint3"], "gather_penalty": kms["k_gather3"]},
         "roofline": roof,

@@ -120,10 +120,22 @@ mgr_status mgr_level_set_images_device(mgr_level *lvl, const float *d_src, const
    warp, evaluate_force, translate, value) plus the penalty's
    value_and_gradient (mia/3d/splinetransformpenalty.cc:60-71, with its
    reference sign).  Any output pointer may be NULL.
-   grad_total = grad_image + grad_penalty, as evaluate_fdf returns it. */
+   grad_total = grad_image + grad_penalty, as evaluate_fdf returns it.
+   Non-finite parameters: MGR_ERR_ARG, and the output buffers are not
+   written. */
 mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad_total,
                               double *grad_image, double *grad_penalty,
                               double *cost_image, double *cost_penalty);
+
+/* How mgr_level_evaluate moves the caller's host data.  *in_place = 1: the
+   level's device reads and writes pageable host memory coherently through
+   the host's page tables (Grace-based systems such as GB300) and the level
+   is a 3D split-path level; the kernels read `params` and write the
+   gradients where the caller holds them, with no staged copy.  *in_place =
+   0: the call stages them through device buffers.  MGR_HOST_COPY=1 in the
+   environment when the level is created keeps the staged copies.  The
+   results are the same bit for bit.  Has no counterpart in the reference. */
+mgr_status mgr_level_host_access(const mgr_level *lvl, int *in_place);
 
 /* Device variant: params / grad_total are device pointers (nparams doubles),
    d_costs receives {cost_image, cost_penalty} (2 doubles, device).  The

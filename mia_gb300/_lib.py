@@ -33,6 +33,7 @@ SIGNATURES = {
     "mgr_level_set_images": (ctypes.c_int, [_vp, _fp, _fp]),
     "mgr_level_set_images_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "mgr_level_evaluate": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "mgr_level_host_access": (ctypes.c_int, [_vp, _ip]),
     "mgr_level_evaluate_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "mgr_level_value": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "mgr_level_warp": (ctypes.c_int, [_vp, _dp, _fp]),

@@ -234,6 +234,7 @@ mgr_level *level_create_on_images(const mgr_level *S, const int csize[3], cudaSt
     L->nparams = L->ncoef * D;
     L->path = S->path;
     L->device = S->device;
+    L->coherent = S->coherent;
     L->stream = st;
     L->images_from = S;
     L->images_set = true;
@@ -304,6 +305,7 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         L->device = device;
         ck(cudaSetDevice(device), "cudaSetDevice");
         configure_pool(device);
+        L->coherent = coherent_host_access(device);
         if (stream) {
             L->stream = static_cast<cudaStream_t>(stream);
         } else {
@@ -439,6 +441,39 @@ static void upload_params(mgr_level *L, const double *params)
     }
 }
 
+static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient);
+
+// Evaluation on a device that reads and writes the caller's host memory
+// coherently (3D split path): the parameter conversion reads the caller's
+// parameters, the gather writes the gradients into the caller's buffers and
+// the costs and status flags into the level's pinned buffer; no staged copy
+// and one synchronisation.  Non-finite parameters are found by the
+// conversion: the kernels then run on zeros in their place, nothing is
+// written to the caller's buffers and the call fails as the staged path does.
+static void evaluate_in_place(mgr_level *L, const double *params, double *grad_total, double *grad_image,
+                              double *grad_penalty, double *cost_image, double *cost_penalty)
+{
+    EvalArgs a = L->args();
+    a.params_host = params;
+    if (grad_total) a.grad_total = grad_total;
+    a.grad_image = grad_image;
+    a.grad_penalty = grad_penalty;
+    double *hc = L->host_small();
+    a.host_out = hc;
+    run_image_term(L, a, true);
+    check_launch("evaluate kernels");
+    ck(cudaStreamSynchronize(L->stream), "evaluate sync");
+    unsigned flags[2];
+    std::memcpy(flags, hc + 2, sizeof flags);
+    if (flags[1]) {
+        if (flags[0]) ck(cudaMemsetAsync(L->counters.p + 6, 0, sizeof(unsigned), L->stream), "status reset");
+        throw std::invalid_argument("parameters must be finite");
+    }
+    throw_if_flagged(L, flags[0]);
+    if (cost_image) *cost_image = hc[0];
+    if (cost_penalty) *cost_penalty = hc[1];
+}
+
 static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
 {
     cudaStream_t st = L->stream;
@@ -551,6 +586,10 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
     return guarded([&] {
         if (!lvl->images_set) throw StateError("set_images must be called before evaluate");
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        if (lvl->coherent && lvl->d.dim == 3 && lvl->path == MGR_PATH_SPLIT) {
+            evaluate_in_place(lvl, params, grad_total, grad_image, grad_penalty, cost_image, cost_penalty);
+            return;
+        }
         upload_params(lvl, params);
         EvalArgs a = lvl->args();
         if (grad_image && lvl->path != MGR_PATH_PLAIN) {
@@ -581,6 +620,13 @@ mgr_status mgr_level_evaluate(mgr_level *lvl, const double *params, double *grad
         if (cost_image) *cost_image = hc[0];
         if (cost_penalty) *cost_penalty = hc[1];
     });
+}
+
+mgr_status mgr_level_host_access(const mgr_level *lvl, int *in_place)
+{
+    if (!lvl || !in_place) return fail(MGR_ERR_ARG, "null argument");
+    *in_place = lvl->coherent && lvl->d.dim == 3 && lvl->path == MGR_PATH_SPLIT ? 1 : 0;
+    return MGR_OK;
 }
 
 mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_image, double *cost_penalty)

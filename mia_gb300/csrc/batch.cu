@@ -726,16 +726,7 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         // caller's arrays where they are, with no staged copy (the host path
         // then costs two reads of the images over the CPU-GPU link);
         // MGR_HOST_COPY=1 keeps the copies
-        bool direct = false;
-        if (!images_on_device) {
-            int pageable = 0, host_tables = 0;
-            const char *force_copy = std::getenv("MGR_HOST_COPY");
-            if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
-                cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) ==
-                    cudaSuccess)
-                direct = pageable == 1 && host_tables == 1 && !(force_copy && *force_copy && *force_copy != '0');
-            cudaGetLastError();
-        }
+        const bool direct = !images_on_device && coherent_host_access(device);
         trace_count("batch: images read in place (1 = yes)", direct ? 1.0 : 0.0);
         for (int p = 0; p < npairs; ++p) {
             std::unique_ptr<PairRun> r(new PairRun);

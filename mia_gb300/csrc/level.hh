@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -160,6 +161,10 @@ struct mgr_level {
     bool images_set = false;
     bool tables_valid = false;
     bool timing = false;
+    // the device reads and writes the caller's host memory in place
+    // (coherent_host_access): evaluate moves parameters, gradient and costs
+    // with the kernels' own loads and stores instead of staged copies
+    bool coherent = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_recorded = false;
     // move the level to stream s: its later work and the stream-ordered
@@ -388,6 +393,21 @@ mgr_level *level_create_on_images(const mgr_level *S, const int csize[3], cudaSt
 }  // namespace mgr
 
 namespace mgr {
+// True when the device reads and writes pageable host memory coherently,
+// translating through the host's page tables (Grace-based systems such as
+// GB300, where the CPU-GPU link is cache coherent), unless the environment
+// variable MGR_HOST_COPY is set to a value other than 0 (staged copies).
+inline bool coherent_host_access(int device)
+{
+    int pageable = 0, host_tables = 0;
+    const char *force_copy = std::getenv("MGR_HOST_COPY");
+    bool ok = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
+              cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) ==
+                  cudaSuccess;
+    cudaGetLastError();
+    return ok && pageable == 1 && host_tables == 1 && !(force_copy && *force_copy && *force_copy != '0');
+}
+
 // Queue a read of the level's device status flag (counters[6], raised by a
 // kernel whose bounded wait gave up) into *flag; after the stream has been
 // synchronised, throw_if_flagged clears it and throws TimeoutError.

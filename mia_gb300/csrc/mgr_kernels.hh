@@ -82,6 +82,13 @@ struct EvalArgs {
     double *grad_image;    // optional
     double *grad_penalty;  // optional
     double *costs;         // optional {cost_image, cost_penalty}
+    // caller's host memory read and written in place (a device with
+    // coherent access to pageable host memory, 3D split path): params_host
+    // is read by the parameter conversion (launch_params_f32), and the
+    // gather's last block writes {cost_image, cost_penalty, status flags}
+    // to host_out; the gradient pointers above may then be host memory too
+    const double *params_host;
+    double *host_out;
 };
 
 // SPLIT path: warp (+cost sums), gradient/force/adjoint, gather(+penalty)

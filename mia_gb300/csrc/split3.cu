@@ -882,7 +882,10 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 gp[1] = pw * (v9[7] + (2.0f * v9[2] + v9[3]));
                 gp[2] = pw * (v9[8] + (2.0f * v9[4] + v9[5]));
             }
-            if (with_gradient) {
+            // parameters the conversion found non-finite: nothing is written
+            // to the caller's buffers
+            const bool bad = a.params_host && *(volatile unsigned *)&a.counters[7] != 0u;
+            if (with_gradient && !bad) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const double gi = image_from_dense ? a.grad_image[i * 3 + k] : double(cw * -v9[9 + k]);
@@ -916,6 +919,17 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             if (a.costs) {
                 a.costs[0] = sc[SC_COST_IMG];
                 a.costs[1] = sc[SC_COST_PEN];
+            }
+            if (a.host_out) {
+                // the costs and both status flags to the caller's host
+                // memory; the non-finite flag is cleared for the next call
+                // (every block has read it before its arrival above)
+                a.host_out[0] = sc[SC_COST_IMG];
+                a.host_out[1] = sc[SC_COST_PEN];
+                unsigned *hf = reinterpret_cast<unsigned *>(a.host_out + 2);
+                hf[0] = *(volatile unsigned *)&a.counters[6];
+                hf[1] = *(volatile unsigned *)&a.counters[7];
+                a.counters[7] = 0;
             }
             a.counters[1] = 0;
         }
@@ -1065,11 +1079,36 @@ __global__ void __launch_bounds__(256) k_params_f32(const double *__restrict__ p
 // ---------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------
+// The parameters read where the caller holds them (host memory that the
+// device reads coherently): the device keeps a double and a float copy.  A
+// non-finite value is stored as 0 in both and raises counters[7], so that
+// the kernels after it run on finite parameters and the gather writes
+// nothing to the caller's buffers.
+__global__ void __launch_bounds__(256) k_params_host(const double *__restrict__ src, double *__restrict__ p,
+                                                     float *__restrict__ f, size_t n, unsigned *__restrict__ bad)
+{
+    bool nonfinite = false;
+    for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) {
+        double v = src[i];
+        if (!isfinite(v)) {
+            nonfinite = true;
+            v = 0.0;
+        }
+        p[i] = v;
+        f[i] = float(v);
+    }
+    if (__any_sync(FULL, nonfinite) && (threadIdx.x & 31) == 0) atomicOr(bad, 1u);
+}
+
 void launch_params_f32(const EvalArgs &a, cudaStream_t st)
 {
     const size_t n = size_t(a.nc[0]) * a.nc[1] * a.nc[2] * 3;
     const int nb = int(std::min<size_t>(1024, (n + 255) / 256));
-    k_params_f32<<<nb, 256, 0, st>>>(a.params, a.params_f, n);
+    if (a.params_host)
+        k_params_host<<<nb, 256, 0, st>>>(a.params_host, const_cast<double *>(a.params), a.params_f, n,
+                                          a.counters + 7);
+    else
+        k_params_f32<<<nb, 256, 0, st>>>(a.params, a.params_f, n);
     count_launch();
 }
 size_t split3_smem(const EvalArgs &a, int which)

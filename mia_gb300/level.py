@@ -119,6 +119,15 @@ class Level:
         check(lib().mgr_level_tile(self.h, t))
         return tuple(t)
 
+    @property
+    def in_place(self):
+        """True when evaluate reads the parameters and writes the gradients
+        in the caller's host memory (coherent host access), False when it
+        stages them through device buffers"""
+        v = ctypes.c_int(0)
+        check(lib().mgr_level_host_access(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_images(self, src, ref):
         s, r = _f(src), _f(ref)
         if s.shape != self.shape or r.shape != self.shape:

@@ -487,3 +487,47 @@ def test_bound_evaluate_call_equals_evaluate_total():
     assert e.value.status == _lib.MGR_ERR_ARG
     params[3] = 0.0
     assert np.isfinite(call())
+
+
+@pytest.mark.parametrize("cost,size", [("ssd", (33, 29, 21)), ("ncc", (70, 41, 37))])
+def test_in_place_evaluation_equals_staged_copies(cost, size):
+    """evaluate with the caller's host buffers read and written in place by
+    the kernels (coherent host access, Grace-based hosts) gives the staged
+    copies' costs and gradients bit for bit; non-finite parameters are
+    refused without touching the caller's buffers, and the level keeps
+    working"""
+    import os
+    import platform
+    import mia_gb300 as M
+    from mia_gb300 import _lib
+    from mia_gb300 import synth
+    kw = dict(rate=5.0, cost=cost, penalty_weight=3.0)
+    lv = M.Level(size, **kw)
+    os.environ["MGR_HOST_COPY"] = "1"
+    try:
+        staged = M.Level(size, **kw)
+    finally:
+        del os.environ["MGR_HOST_COPY"]
+    assert not staged.in_place
+    if platform.machine() == "aarch64":
+        assert lv.in_place      # Grace: the device reads pageable host memory
+    a, b = make_pair(size[::-1], 9)
+    lv.set_images(a, b)
+    staged.set_images(a, b)
+    for seed in (3, 4):
+        p = synth.smooth_params(lv.csize, 1.5, seed=seed)
+        got, want = lv.evaluate(p), staged.evaluate(p)
+        for g, w in zip(got, want):
+            assert np.array_equal(np.asarray(g), np.asarray(w))
+    params = synth.smooth_params(lv.csize, 1.0, seed=5)
+    grad = np.full(lv.nparams, 7.0)
+    call = lv.bind_evaluate_total(params, grad)
+    params[lv.nparams - 1] = np.inf
+    with pytest.raises(_lib.MgrError) as e:
+        call()
+    assert e.value.status == _lib.MGR_ERR_ARG
+    assert np.all(grad == 7.0)
+    params[lv.nparams - 1] = 0.0
+    c = call()
+    want_c, want_g = staged.evaluate_total(params.copy())
+    assert c == want_c and np.array_equal(grad, want_g)
