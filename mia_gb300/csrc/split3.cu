@@ -43,6 +43,18 @@
 #include "mgr_cost.cuh"
 #include "warp3_common.cuh"
 
+// the one-pair adjoint kernel: minimum resident blocks per SM (a cap of 40
+// registers, no spills) and the unroll factor of its plane walk (measured
+// at 192x192x128 SSD and 256^3 NCC against no unroll and no cap; the
+// batched kernels keep both off)
+#ifndef MGR_ADJ_MINB
+#define MGR_ADJ_MINB 6
+#endif
+#define MGR_ADJ_BOUNDS __launch_bounds__(NT3, MGR_ADJ_MINB)
+#ifndef MGR_ADJ_UNROLL
+#define MGR_ADJ_UNROLL 2
+#endif
+
 namespace mgr {
 
 void set_last_error(const std::string &msg);
@@ -314,8 +326,14 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const bool staged = boxs[0] != 0;
     const int bxs = boxs[1], bylo = boxs[2], bzbase = boxs[3], nplanes = boxs[4], span = boxs[5];
-    const int bw4 = boxs[6], brows = boxs[7];
+    const int brows = boxs[7];
     bool ring_ok = staged;
+    // planes (bit t) of this thread's voxels whose taps are not read from
+    // the ring: all of them when the tile was not staged, else the rare
+    // voxel outside the box and, after a wait gave up, the rest of the walk.
+    // They are sampled from global memory after the walk, so that the walk
+    // itself makes no call (a call site costs the loop register spills).
+    unsigned defer = 0u;
     int kwait = 0;      // planes below kwait have arrived
     // the reference is streamed three planes ahead of its use (registers
     // r0..r2), so the walk does not wait on its memory latency
@@ -330,15 +348,18 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         if (ez > 2) r2 = __ldg(rin + 2 * nxy);
         if (ez > 3) r3 = __ldg(rin + 3 * nxy);
     }
-    auto sample = [&](int t, const float u[3]) -> float {
+    // the sample at plane t from the ring; ok = false when its taps are
+    // not there (the voxel is deferred)
+    auto sample_ring = [&](int t, const float u[3], bool &ok) -> float {
         const int z = z0 + t;
         const float px = px0 - u[0], py = py0 - u[1], pz = float(z) - u[2];
         const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
         const int col = fx - 1 - bxs, row = fy - 1 - bylo, kk = fz - 1 - bzbase;
-        if (ring_ok && unsigned(col) < unsigned(bw4 - 3) && unsigned(row) < unsigned(brows - 3) &&
-            unsigned(kk - t) < unsigned(span - 3))
+        ok = ring_ok && unsigned(col) < unsigned(RING_X - 3) && unsigned(row) < unsigned(brows - 3) &&
+             unsigned(kk - t) < unsigned(span - 3);
+        if (ok)
             return taps3_ring(ring, ring_slot(kk), row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
-        return taps3_global(a, px, py, pz, mn, mxv);
+        return 0.0f;
     };
     auto add_cost = [&](float wv, float b) {
         if (a.cost == 0) {
@@ -370,7 +391,8 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             }
         }
     };
-    for (int t = 0; t < ez; t += 2) {
+    if (!staged && inxy) defer = ez >= 32 ? ~0u : (1u << ez) - 1u;
+    for (int t = 0; staged && t < ez; t += 2) {
         const bool two = t + 1 < ez;
         float ua[3], ub[3] = {0.0f, 0.0f, 0.0f};
         advance(t);
@@ -400,14 +422,23 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             }
         }
         if (inxy) {
-            const float wa = sample(t, ua);
+            bool oka, okb = true;
+            const float wa = sample_ring(t, ua, oka);
             float wb = 0.0f;
-            if (two) wb = sample(t + 1, ub);
-            wout[0] = wa;
-            add_cost(wa, r0);
+            if (two) wb = sample_ring(t + 1, ub, okb);
+            if (oka) {
+                wout[0] = wa;
+                add_cost(wa, r0);
+            } else {
+                defer |= 1u << t;
+            }
             if (two) {
-                wout[nxy] = wb;
-                add_cost(wb, r1);
+                if (okb) {
+                    wout[nxy] = wb;
+                    add_cost(wb, r1);
+                } else {
+                    defer |= 1u << (t + 1);
+                }
             }
         }
         r0 = r2;
@@ -418,6 +449,26 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         rin += 2 * nxy;
         release(t);
         if (two) release(t + 1);
+    }
+    // the deferred voxels, in plane order: the displacement from the y
+    // stage's window at plane t (the walk's values: the window then starts
+    // at coefficient zs[t]) and the taps from global memory
+    if (defer) {
+        float *const w0p = a.warped + col;
+        const float *const r0p = a.ref + col;
+        do {
+            const int t = __ffs(defer) - 1;
+            defer &= defer - 1u;
+            const int s = zs[t];
+            const float4 wz = zw[t];
+            float u[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                u[c] = wz.x * qat(c, s) + wz.y * qat(c, s + 1) + wz.z * qat(c, s + 2) + wz.w * qat(c, s + 3);
+            const float wv = taps3_global(a, px0 - u[0], py0 - u[1], float(z0 + t) - u[2], mn, mxv);
+            w0p[size_t(t) * nxy] = wv;
+            add_cost(wv, __ldg(r0p + size_t(t) * nxy));
+        } while (defer);
     }
     if (staged) __syncthreads();   // every warp is done with the ring
     if (staged && tid == 0) {
@@ -468,7 +519,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
 // ---------------------------------------------------------------------
 // gradient + force + adjoint
 // ---------------------------------------------------------------------
-template <int TZ>
+template <int TZ, int UNROLL>
 __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by, int bz, int tile_index)
 {
     extern __shared__ __align__(16) float sm3[];
@@ -530,6 +581,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         for (int k = 0; k < 4; ++k) acc[c][k] = 0.0f;
     int cur = 0;   // azs[0] == 0
     auto emit = [&](int kz, int c, float v) { Az[((c * AZc + kz) * TY3 + wy) * TX3 + lane] = v; };
+#pragma unroll UNROLL
     for (int t = 0; t < ez; ++t) {
         const int z = z0 + t;
         const float wp = (z + 1 < nz) ? __ldg(wc + nxy) : 0.0f;
@@ -659,16 +711,30 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
 // ---------------------------------------------------------------------
 // gather + penalty
 // ---------------------------------------------------------------------
+#ifndef MGR_GATHER_THREADS
+#define MGR_GATHER_THREADS 256
+#endif
+#ifdef MGR_GATHER_MINB
+#define MGR_GATHER_BOUNDS __launch_bounds__(MGR_GATHER_THREADS, MGR_GATHER_MINB)
+#else
+#define MGR_GATHER_BOUNDS __launch_bounds__(MGR_GATHER_THREADS)
+#endif
 namespace {
-constexpr int GT3 = 256;
+constexpr int GT3 = MGR_GATHER_THREADS;
 constexpr int GBX = 4, GBY = 4, GBZ = 2;   // coefficients per block: 32, lane = coefficient
 constexpr int GH = 3;                      // stencil half width
 constexpr int GPX = GBX + 2 * GH;          // 10: halo tile edges
 constexpr int GPY = GBY + 2 * GH;          // 10
 constexpr int GPZ = GBZ + 2 * GH;          // 8
 constexpr int GPP = 12;                    // padded row pitch (float4) of the halo tile
-constexpr int GSUB = GT3 / 32;             // 8 warps split each coefficient's work
+constexpr int GSUB = GT3 / 32;             // the warps split each coefficient's work
 constexpr int GNQ = 12;                    // per-warp partials: 9 penalty products, 3 image sums
+constexpr int GSMAX = 64 / GSUB;           // partial slots per warp loaded in the first batch
+// the per-warp partials fit beside the halo tables at 8 warps; with more
+// warps they take the tables' place once the stencil is summed
+constexpr int GTAB = GPZ * GPY * GPP + 343 * 2;   // float4: Ps, then Pt
+constexpr bool GALIAS = GSUB * GNQ * 32 > 12 * 32 * 8;
+static_assert(!GALIAS || GSUB * GNQ * 32 <= 4 * GTAB, "partials must fit in the tables' space");
 }  // namespace
 
 // Block: 4 x 4 x 2 coefficients, one per lane; the 8 warps split the 49
@@ -679,13 +745,13 @@ constexpr int GNQ = 12;                    // per-warp partials: 9 penalty produ
 __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradient, int image_from_dense, int blk,
                                              int nblk)
 {
-    __shared__ float4 Ps[GPZ * GPY * GPP];
-    __shared__ float4 Pt[343 * 2];
-    __shared__ float pacc[GSUB][GNQ][32];
+    __shared__ float4 PsPt[GTAB];
+    __shared__ float pacc_own[GALIAS ? 1 : GSUB * GNQ * 32];
     __shared__ int gl[3][GBX][GATHER_LMAX];
     __shared__ int gn[3][GBX];
-    __shared__ float wred[GSUB];
     __shared__ bool is_last;
+    float4 *Ps = PsPt, *Pt = PsPt + GPZ * GPY * GPP;
+    float (*pacc)[GNQ][32] = reinterpret_cast<float (*)[GNQ][32]>(GALIAS ? reinterpret_cast<float *>(PsPt) : pacc_own);
     const Axis &X = a.ax[0], &Y = a.ax[1], &Z = a.ax[2];
     const int ncx = a.nc[0], ncy = a.nc[1], ncz = a.nc[2];
     const int nbx = (ncx + GBX - 1) / GBX, nby = (ncy + GBY - 1) / GBY;
@@ -762,7 +828,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
 
     // batch 2: this warp's share of the partial slots (entries k = w,
     // w + 8, ...) of the lane's coefficient, issued before the stencil
-    constexpr int SMAX = 8;
+    constexpr int SMAX = GSMAX;
     float sv[SMAX][3];
     int tot = 0, nX = 0, nY = 0, nZ = 0;
     bool lists = false;
@@ -842,6 +908,16 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             }
         }
     }
+    // the lane's own parameters (the penalty value), read before the
+    // partials may take the tables' place
+    float ci[3] = {0.0f, 0.0f, 0.0f};
+    if (w == 0 && a.has_penalty) {
+        const float4 c4 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)];
+        ci[0] = c4.x;
+        ci[1] = c4.y;
+        ci[2] = c4.z;
+    }
+    if (GALIAS) __syncthreads();
     pacc[w][0][lane] = R0;
     pacc[w][1][lane] = R1;
     pacc[w][2][lane] = R2;
@@ -855,25 +931,26 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     pacc[w][10][lane] = S1;
     pacc[w][11][lane] = S2;
     __syncthreads();
-    // warp 0 combines the warps' partials in a fixed order (FP32; the
-    // outputs are widened to double at the store)
+    // the warps' partials of each quantity summed in a fixed order (FP32,
+    // warp k % GSUB sums quantity k into row 0), then warp 0 combines them
+    // (the outputs are widened to double at the store)
+    for (int k = w; k < GNQ; k += GSUB) {
+        float t = pacc[0][k][lane];
+#pragma unroll
+        for (int ww = 1; ww < GSUB; ++ww) t += pacc[ww][k][lane];
+        pacc[0][k][lane] = t;
+    }
+    __syncthreads();
     if (w == 0) {
         float pval = 0.0f;
         if (valid) {
             float v9[GNQ];
 #pragma unroll
-            for (int k = 0; k < GNQ; ++k) {
-                float t = pacc[0][k][lane];
-#pragma unroll
-                for (int ww = 1; ww < GSUB; ++ww) t += pacc[ww][k][lane];
-                v9[k] = t;
-            }
+            for (int k = 0; k < GNQ; ++k) v9[k] = pacc[0][k][lane];
             float gp[3] = {0.0f, 0.0f, 0.0f};
             const float pw = float(a.pen_grad_sign * a.pen_weight), cw = float(a.cost_weight);
             if (a.has_penalty) {
-                const float ci0 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].x;
-                const float ci1 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].y;
-                const float ci2 = Ps[((lz + GH) * GPY + (ly + GH)) * GPP + (lx + GH)].z;
+                const float ci0 = ci[0], ci1 = ci[1], ci2 = ci[2];
                 if (with_gradient)
                     pval = ci0 * v9[0] + ci0 * v9[1] + ci1 * v9[2] + ci1 * v9[3] + ci2 * v9[4] + ci2 * v9[5];
                 else
@@ -952,13 +1029,13 @@ __global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3(const __grid_const
 }
 
 template <int TZ>
-__global__ void __launch_bounds__(NT3) k_adjoint3(EvalArgs a)
+__global__ void MGR_ADJ_BOUNDS k_adjoint3(EvalArgs a)
 {
     const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    adjoint3_body<TZ>(a, blockIdx.x, blockIdx.y, blockIdx.z, tile);
+    adjoint3_body<TZ, MGR_ADJ_UNROLL>(a, blockIdx.x, blockIdx.y, blockIdx.z, tile);
 }
 
-__global__ void __launch_bounds__(GT3) k_gather3(EvalArgs a, int with_gradient, int image_from_dense)
+__global__ void MGR_GATHER_BOUNDS k_gather3(EvalArgs a, int with_gradient, int image_from_dense)
 {
     gather3_body(a, with_gradient, image_from_dense, blockIdx.x, gridDim.x);
 }
@@ -994,7 +1071,7 @@ __global__ void __launch_bounds__(NT3) k_adjoint3_batch(const EvalArgs *__restri
     const EvalArgs &a = args[it.x];
     int bx, by, bz, nt;
     decode_tile3(a, it.y, bx, by, bz, nt);
-    adjoint3_body<TZ>(a, bx, by, bz, it.y);
+    adjoint3_body<TZ, 1>(a, bx, by, bz, it.y);
 }
 
 // Persistent forms of the batched warp and adjoint kernels: a grid of
@@ -1054,12 +1131,12 @@ __global__ void __launch_bounds__(NT3) k_adjoint3_queue(const EvalArgs *__restri
         const EvalArgs &a = args[it.x];
         int bx, by, bz, nt;
         decode_tile3(a, it.y, bx, by, bz, nt);
-        adjoint3_body<TZ>(a, bx, by, bz, it.y);
+        adjoint3_body<TZ, 1>(a, bx, by, bz, it.y);
     }
     queue_done(queue);
 }
 
-__global__ void __launch_bounds__(GT3) k_gather3_batch(const EvalArgs *__restrict__ args,
+__global__ void MGR_GATHER_BOUNDS k_gather3_batch(const EvalArgs *__restrict__ args,
                                                        const int2 *__restrict__ items, const int *__restrict__ active,
                                                        const int *__restrict__ nblocks)
 {
