@@ -142,11 +142,13 @@ def cpu_baseline(w, mov, ref, params, seconds, threads):
     return N * n / dt / 1e6, n, dt, res
 
 
-def time_evals(lv, p_d, g_d, c_d, flush, steps, warmup=2):
-    """device ms of one cost+gradient evaluation (the level's own events,
-    L2 flushed before each), mean over `steps`"""
+def time_evals(lv, p_d, g_d, c_d, flush, steps, warmup=2, per_kernel=False):
+    """device ms of one cost+gradient evaluation (the level's own events
+    around the whole evaluation, L2 flushed before each), mean over `steps`;
+    per_kernel: the mean (warp, adjoint, gather, total) with events around
+    every kernel (the kernels then run one after another)"""
     import torch
-    lv.set_timing(True)
+    lv.set_timing(True, whole=not per_kernel)
     for _ in range(warmup):
         lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
     lv.sync()
@@ -156,8 +158,9 @@ def time_evals(lv, p_d, g_d, c_d, flush, steps, warmup=2):
         torch.cuda.synchronize()
         lv.evaluate_device(p_d.data_ptr(), g_d.data_ptr(), c_d.data_ptr())
         lv.sync()
-        per.append(lv.kernel_times()[3])
-    return float(np.mean(per))
+        per.append(lv.kernel_times())
+    per = np.array(per)
+    return tuple(float(v) for v in per.mean(axis=0)) if per_kernel else float(per[:, 3].mean())
 
 
 def split_vs_plain(lv, p_d, g_d, c_d, flush, steps, N):
@@ -177,11 +180,11 @@ def fused_vs_split(lv, p_d, g_d, c_d, flush, steps, N, params, tz=16):
     MGR_PATH_FUSED) against the split kernels, same GPU, same inputs: device
     ms per evaluation and the fused result's difference from the split one"""
     t_split = time_evals(lv, p_d, g_d, c_d, flush, steps)
-    k_split = lv.kernel_times()
+    k_split = time_evals(lv, p_d, g_d, c_d, flush, steps, per_kernel=True)
     ref = lv.evaluate(params)
     lv.set_path("fused", (0, 0, tz))
     t_fused = time_evals(lv, p_d, g_d, c_d, flush, steps)
-    k_fused = lv.kernel_times()
+    k_fused = time_evals(lv, p_d, g_d, c_d, flush, steps, per_kernel=True)
     got = lv.evaluate(params)
     lv.set_path("split")
     return {"split_ms": t_split, "fused_ms": t_fused, "speedup_fused_vs_split": t_split / t_fused,
@@ -606,7 +609,9 @@ def run_gpu(args):
     g_d = torch.empty(nparams, dtype=torch.float64, device=dev)
     c_d = torch.empty(2, dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    lv.set_timing(True)
+    # events around the whole evaluation: its kernels overlap as in an
+    # untimed run (programmatic dependent launch)
+    lv.set_timing(True, whole=True)
     torch.cuda.synchronize()
 
     barrier = replicas.barrier
@@ -630,6 +635,9 @@ def run_gpu(args):
     launches = M.lib().mgr_kernel_launch_count() - launches0
     per = np.array(per)
     value, t_step = replicas.whole_job_rate(N / 1e6, per[:, 3].mean() / 1e3, ws, device=dev)
+    # the kernels' own times, from a second pass with events around each
+    # kernel (which then run one after another)
+    per_k = np.array(time_evals(lv, p_d, g_d, c_d, flush, args.steps, per_kernel=True))[None, :]
 
     # end to end through the C ABI: host (pinned) params in, gradient out;
     # on a host whose memory the device reads coherently the kernels move
@@ -659,8 +667,8 @@ def run_gpu(args):
     # written as double (4 + 8 B per parameter)
     b_eval = 8.0 * N + 12.0 * D * C
     peak, peak_kind = measured_peaks()
-    kms = {"k_warp3": float(per[:, 0].mean()), "k_adjoint3": float(per[:, 1].mean()),
-           "k_gather3": float(per[:, 2].mean())}
+    kms = {"k_warp3": float(per_k[:, 0].mean()), "k_adjoint3": float(per_k[:, 1].mean()),
+           "k_gather3": float(per_k[:, 2].mean())}
     top = max(kms, key=kms.get)
     t_top = kms[top] / 1e3
     roof = {"bound": "hbm", "kernel": top, "achieved": b_eval / t_top / 1e9, "peak": peak,

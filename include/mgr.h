@@ -176,13 +176,17 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
    given to mgr_level_set_path. */
 mgr_status mgr_level_tile(const mgr_level *lvl, int tile[3]);
 
-/* Kernel timing for profiling: with `enable` set, every evaluation records
-   CUDA events around its kernels on the level's stream.
+/* Kernel timing for profiling: with `enable` = 1, every evaluation records
+   CUDA events around each of its kernels on the level's stream (the
+   kernels then run one after another); with `enable` = 2, events around the
+   whole evaluation only (the 3D split path's kernels keep their overlapped
+   launches, as in an untimed evaluation); 0 turns timing off.
    mgr_level_kernel_times waits for the last evaluation and writes the
    device time in milliseconds of its kernels: ms[0] warp, ms[1]
    gradient/force/adjoint, ms[2] gather+penalty, ms[3] the whole image and
-   penalty term (plain path: ms[3] only).  Has no counterpart in the
-   reference (it replaces its optional TRACE logging of timings). */
+   penalty term (plain path and `enable` = 2: ms[3] only, the others 0).
+   Has no counterpart in the reference (it replaces its optional TRACE
+   logging of timings). */
 mgr_status mgr_level_set_timing(mgr_level *lvl, int enable);
 mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4]);
 

@@ -235,6 +235,7 @@ mgr_level *level_create_on_images(const mgr_level *S, const int csize[3], cudaSt
     L->path = S->path;
     L->device = S->device;
     L->coherent = S->coherent;
+    L->pdl = S->pdl;
     L->stream = st;
     L->images_from = S;
     L->images_set = true;
@@ -306,6 +307,10 @@ mgr_status mgr_level_create(const mgr_level_desc *desc, int device, void *stream
         ck(cudaSetDevice(device), "cudaSetDevice");
         configure_pool(device);
         L->coherent = coherent_host_access(device);
+        {
+            const char *e = std::getenv("MGR_PDL");
+            L->pdl = !(e && std::strcmp(e, "0") == 0);
+        }
         if (stream) {
             L->stream = static_cast<cudaStream_t>(stream);
         } else {
@@ -482,6 +487,7 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         return;
     }
     L->ev_recorded = L->timing;
+    L->ev_mode = L->timing_mode;
     if (L->path == MGR_PATH_FUSED) {
         // the fused kernel and the gather on the fused tiles' tables; the
         // call's buffers as the caller set them in a
@@ -794,10 +800,12 @@ mgr_status mgr_level_set_timing(mgr_level *lvl, int enable)
     if (!lvl) return fail(MGR_ERR_ARG, "null level");
     return guarded([&] {
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
+        if (enable < 0 || enable > 2) throw std::invalid_argument("timing mode must be 0, 1 or 2");
         if (enable)
             for (auto &e : lvl->ev)
                 if (!e) ck(cudaEventCreate(&e), "cudaEventCreate");
         lvl->timing = enable != 0;
+        lvl->timing_mode = enable;
     });
 }
 
@@ -810,6 +818,8 @@ mgr_status mgr_level_kernel_times(mgr_level *lvl, double ms[4])
         ck(cudaEventSynchronize(lvl->ev[3]), "cudaEventSynchronize");
         float t;
         for (int k = 0; k < 3; ++k) {
+            ms[k] = 0.0;
+            if (lvl->ev_mode != 1) continue;   // whole-evaluation events only
             ck(cudaEventElapsedTime(&t, lvl->ev[k], lvl->ev[k + 1]), "elapsed");
             ms[k] = t;
         }

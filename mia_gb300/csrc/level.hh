@@ -161,6 +161,12 @@ struct mgr_level {
     bool images_set = false;
     bool tables_valid = false;
     bool timing = false;
+    // 1: events around every kernel (launched one after another); 2: events
+    // around the whole evaluation only (kernels overlap as in untimed runs)
+    int timing_mode = 0, ev_mode = 0;
+    // programmatic dependent launch of the split path's kernels (MGR_PDL=0
+    // in the environment at level creation turns it off)
+    bool pdl = true;
     // the device reads and writes the caller's host memory in place
     // (coherent_host_access): evaluate moves parameters, gradient and costs
     // with the kernels' own loads and stores instead of staged copies
@@ -189,7 +195,7 @@ struct mgr_level {
     }
     void record(int k)
     {
-        if (timing) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");
+        if (timing && (timing_mode == 1 || k == 0 || k == 3)) ck(cudaEventRecord(ev[k], stream), "cudaEventRecord");
     }
     // 4 doubles of pinned host memory for small read-backs (costs, status)
     double *host_small_p = nullptr;
@@ -240,6 +246,7 @@ struct mgr_level {
         a.slot = fused ? slot_f : slot;
         a.tile_sums = tile_sums.p;
         a.counters = counters.p;
+        a.pdl = pdl && timing_mode != 1;
         a.scalars = scalars.p;
         a.has_penalty = d.has_penalty;
         double prod = double(d.size[0]) * d.size[1] * (d.dim == 3 ? d.size[2] : 1);

@@ -89,6 +89,10 @@ struct EvalArgs {
     // to host_out; the gradient pointers above may then be host memory too
     const double *params_host;
     double *host_out;
+    // 1: the 3D split path's warp, adjoint and gather kernels are launched
+    // with programmatic stream serialisation (each may start while the one
+    // before it finishes, and waits for it before reading its outputs)
+    int pdl;
 };
 
 // SPLIT path: warp (+cost sums), gradient/force/adjoint, gather(+penalty)

@@ -66,6 +66,23 @@ constexpr int TX3 = 32;    // tile x (lanes)
 constexpr int TY3 = 8;     // tile y (warps)
 constexpr unsigned FULL = 0xffffffffu;
 
+// Programmatic dependent launch.  A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while the
+// kernel before it in the stream is still running; pdl_wait returns once
+// that kernel has completed and its writes are visible (at once for a
+// kernel launched without the attribute).  Before it a kernel reads only
+// the level's fixed tables.  pdl_trigger, issued by every block after its
+// pdl_wait, lets the next kernel be launched: so no kernel starts before the
+// one two places back in the stream has completed.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+__device__ __forceinline__ void pdl_trigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------
@@ -114,6 +131,9 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         csc[1] = float(a.centers[1]);
     }
 
+    // the parameters' float copy comes from the kernel before this one
+    pdl_wait();
+    pdl_trigger();
     float *C = sm3;                        // [3][FZ][FY][FX]
     float *Tx = C + 3 * FZ * FY * FX;      // [3][FZ][FY][32]
     // [RING_N][RING_Y][RING_X]: the tensor copies want a 128-byte aligned
@@ -545,17 +565,11 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
     const size_t col = size_t(min(y, ny - 1)) * nx + min(x, nx - 1);
     const float *__restrict__ W = a.warped;
     const float *__restrict__ R = a.ref;
-    if (tid < 5) {
-        const int slot[5] = {SC_K1, SC_K2, SC_MA, SC_MB, SC_FSCALE};
-        fsc[tid] = float(a.scalars[slot[tid]]);
-    }
     const bool bx_in = x > 0 && x < nx - 1, by_in = y > 0 && y < ny - 1;
     // column pointers at the current plane
     const float *__restrict__ wc = W + size_t(z0) * nxy + col;
     const float *__restrict__ rc = R + size_t(z0) * nxy + col;
     const int ynm = (y > 0) ? -nx : 0, ynp = (y + 1 < ny) ? nx : 0;
-    float wm = (z0 > 0) ? __ldg(wc - nxy) : 0.0f;
-    float w0 = __ldg(wc);
     if (tid < TX3) {
         const int xx = min(x0 + tid, nx - 1);
         asx[tid] = X.as[xx] - ax0;
@@ -571,6 +585,15 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         azs[tid] = Z.as[zz] - az0;
         azw[tid] = Z.aw[zz];
     }
+    // the warped image and the cost's scalars come from the warp kernel
+    pdl_wait();
+    pdl_trigger();
+    if (tid < 5) {
+        const int slot[5] = {SC_K1, SC_K2, SC_MA, SC_MB, SC_FSCALE};
+        fsc[tid] = float(a.scalars[slot[tid]]);
+    }
+    float wm = (z0 > 0) ? __ldg(wc - nxy) : 0.0f;
+    float w0 = __ldg(wc);
     __syncthreads();
     const float k1 = fsc[0], k2 = fsc[1], ma = fsc[2], mb = fsc[3], fscale = fsc[4];
 
@@ -776,6 +799,32 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
         }
         gn[ax][k] = cnt;
     }
+    // the penalty cells (fixed tables), then, once the kernels before this
+    // one have completed, the parameters' float copy with its halo
+    if (a.has_penalty) {
+        constexpr int KT = (343 + GT3 - 1) / GT3;
+        float tv[KT][6];
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            const int e = tid + k * GT3;
+            if (e < 343) {
+                const int dx = e % 7 - 3, dy = (e / 7) % 7 - 3, dz = e / 49 - 3;
+                const float *P = a.ptable + (((dz + 4) * 9 + (dy + 4)) * 9 + (dx + 4)) * 6;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) tv[k][j] = P[j];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KT; ++k) {
+            const int e = tid + k * GT3;
+            if (e < 343) {
+                Pt[2 * e] = make_float4(tv[k][0], tv[k][1], tv[k][2], tv[k][3]);
+                Pt[2 * e + 1] = make_float4(tv[k][4], tv[k][5], 0.0f, 0.0f);
+            }
+        }
+    }
+    pdl_wait();
+    pdl_trigger();
     if (a.has_penalty) {
         constexpr int NH = GPX * GPY * GPZ;
         constexpr int KP = (NH + GT3 - 1) / GT3;
@@ -795,32 +844,12 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 }
             }
         }
-        constexpr int KT = (343 + GT3 - 1) / GT3;
-        float tv[KT][6];
-#pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            const int e = tid + k * GT3;
-            if (e < 343) {
-                const int dx = e % 7 - 3, dy = (e / 7) % 7 - 3, dz = e / 49 - 3;
-                const float *P = a.ptable + (((dz + 4) * 9 + (dy + 4)) * 9 + (dx + 4)) * 6;
-#pragma unroll
-                for (int j = 0; j < 6; ++j) tv[k][j] = P[j];
-            }
-        }
 #pragma unroll
         for (int k = 0; k < KP; ++k) {
             const int e = tid + k * GT3;
             if (e < NH) {
                 const int hx = e % GPX, hy = (e / GPX) % GPY, hz = e / (GPX * GPY);
                 Ps[(hz * GPY + hy) * GPP + hx] = make_float4(pv[k][0], pv[k][1], pv[k][2], 0.0f);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < KT; ++k) {
-            const int e = tid + k * GT3;
-            if (e < 343) {
-                Pt[2 * e] = make_float4(tv[k][0], tv[k][1], tv[k][2], tv[k][3]);
-                Pt[2 * e + 1] = make_float4(tv[k][4], tv[k][5], 0.0f, 0.0f);
             }
         }
     }
@@ -1150,12 +1179,33 @@ __global__ void MGR_GATHER_BOUNDS k_gather3_batch(const EvalArgs *__restrict__ a
 // slow on this GPU, so they are done once per evaluation)
 __global__ void __launch_bounds__(256) k_params_f32(const double *__restrict__ p, float *__restrict__ f, size_t n)
 {
+    pdl_trigger();   // the warp kernel may start its set-up (it waits for this kernel)
     for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) f[i] = float(p[i]);
 }
 
 // ---------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------
+// A launch that may start while the kernel before it in the stream is still
+// running (programmatic stream serialisation; the kernel waits in pdl_wait
+// before it reads that kernel's outputs), or a plain stream-ordered launch.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // The parameters read where the caller holds them (host memory that the
 // device reads coherently): the device keeps a double and a float copy.  A
 // non-finite value is stored as 0 in both and raises counters[7], so that
@@ -1164,6 +1214,7 @@ __global__ void __launch_bounds__(256) k_params_f32(const double *__restrict__ p
 __global__ void __launch_bounds__(256) k_params_host(const double *__restrict__ src, double *__restrict__ p,
                                                      float *__restrict__ f, size_t n, unsigned *__restrict__ bad)
 {
+    pdl_trigger();   // the warp kernel may start its set-up (it waits for this kernel)
     bool nonfinite = false;
     for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < n; i += size_t(gridDim.x) * 256) {
         double v = src[i];
@@ -1208,14 +1259,14 @@ template <int TZ>
 void launch_warp3_z(const EvalArgs &a, size_t sm, cudaStream_t st)
 {
     cudaFuncSetAttribute(k_warp3<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_warp3<TZ><<<dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), NT3, sm, st>>>(a);
+    launch_pdl(a.pdl != 0, k_warp3<TZ>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
 }
 
 template <int TZ>
 void launch_adjoint3_z(const EvalArgs &a, size_t sm, cudaStream_t st)
 {
     cudaFuncSetAttribute(k_adjoint3<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    k_adjoint3<TZ><<<dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), NT3, sm, st>>>(a);
+    launch_pdl(a.pdl != 0, k_adjoint3<TZ>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
 }
 
 template <int TZ>
@@ -1293,7 +1344,7 @@ int gather3_blocks(const EvalArgs &a)
 
 void launch_gather3(const EvalArgs &a, int with_gradient, int dense, cudaStream_t st)
 {
-    k_gather3<<<gather3_blocks(a), GT3, 0, st>>>(a, with_gradient, dense);
+    launch_pdl(a.pdl != 0, k_gather3, dim3(gather3_blocks(a)), dim3(GT3), 0, st, a, with_gradient, dense);
     count_launch();
 }
 

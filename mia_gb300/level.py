@@ -219,8 +219,11 @@ class Level:
         check(lib().mgr_level_translate(self.h, f.ctypes.data_as(_fp), g.ctypes.data_as(_dp)))
         return g
 
-    def set_timing(self, enable=True):
-        check(lib().mgr_level_set_timing(self.h, int(enable)))
+    def set_timing(self, enable=True, whole=False):
+        """record CUDA events around every kernel of each evaluation
+        (`whole`: around the whole evaluation only, kernels overlapped as
+        in untimed runs)"""
+        check(lib().mgr_level_set_timing(self.h, (2 if whole else 1) if enable else 0))
 
     def kernel_times(self):
         """device ms of the last evaluation: (warp, adjoint, gather, total)"""

@@ -531,3 +531,46 @@ def test_in_place_evaluation_equals_staged_copies(cost, size):
     c = call()
     want_c, want_g = staged.evaluate_total(params.copy())
     assert c == want_c and np.array_equal(grad, want_g)
+
+
+@pytest.mark.parametrize("cost,size", [("ssd", (70, 41, 37)), ("ncc", (33, 29, 21))])
+def test_overlapped_launches_equal_serial_launches(cost, size):
+    """programmatic dependent launch of the warp, adjoint and gather kernels
+    (each may start while the one before it finishes) gives the results of
+    plain stream-ordered launches (MGR_PDL=0) bit for bit, through evaluate,
+    value and the per-kernel timing mode (which launches them one after
+    another); the whole-evaluation timing mode reports the total only"""
+    import os
+    import mia_gb300 as M
+    from mia_gb300 import _lib
+    from mia_gb300 import synth
+    kw = dict(rate=5.0, cost=cost, penalty_weight=3.0)
+    lv = M.Level(size, **kw)
+    os.environ["MGR_PDL"] = "0"
+    try:
+        serial = M.Level(size, **kw)
+    finally:
+        del os.environ["MGR_PDL"]
+    a, b = make_pair(size[::-1], 11)
+    lv.set_images(a, b)
+    serial.set_images(a, b)
+    for seed in (6, 7):
+        p = synth.smooth_params(lv.csize, 1.5, seed=seed)
+        want = serial.evaluate(p)
+        for mode in (None, "whole", "per_kernel"):
+            if mode is not None:
+                lv.set_timing(True, whole=(mode == "whole"))
+            got = lv.evaluate(p)
+            for g, w in zip(got, want):
+                assert np.array_equal(np.asarray(g), np.asarray(w))
+            if mode == "whole":
+                ms = lv.kernel_times()
+                assert ms[0] == ms[1] == ms[2] == 0.0 and ms[3] > 0.0
+            elif mode == "per_kernel":
+                ms = lv.kernel_times()
+                assert min(ms) > 0.0
+        lv.set_timing(False)
+        assert lv.value(p) == serial.value(p)
+    with pytest.raises(_lib.MgrError) as e:
+        _lib.check(_lib.lib().mgr_level_set_timing(lv.h, 3))
+    assert e.value.status == _lib.MGR_ERR_ARG
