@@ -787,7 +787,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     const size_t i = valid ? (size_t(cz) * ncy + cy) * ncx + cx : 0;
     const bool img = with_gradient && !image_from_dense;
 
-    // batch 1: offset lists, parameters with halo, penalty cells
+    // fixed tables first: offset lists and penalty cells
     if (img && tid < 3 * GBX) {
         const int ax = tid / GBX, k = tid - ax * GBX;
         const Axis &A = a.ax[ax];
@@ -799,8 +799,6 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
         }
         gn[ax][k] = cnt;
     }
-    // the penalty cells (fixed tables), then, once the kernels before this
-    // one have completed, the parameters' float copy with its halo
     if (a.has_penalty) {
         constexpr int KT = (343 + GT3 - 1) / GT3;
         float tv[KT][6];
@@ -823,8 +821,36 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             }
         }
     }
+    __syncthreads();   // the offset lists
     pdl_wait();
     pdl_trigger();
+    // this warp's share of the partial slots (entries k = w, w + GSUB, ...)
+    // of the lane's coefficient and the parameters with their halo: one
+    // batch of independent loads, issued before the stencil
+    constexpr int SMAX = GSMAX;
+    float sv[SMAX][3];
+    int tot = 0, nX = 0, nY = 0, nZ = 0;
+    bool lists = false;
+    if (valid && img) {
+        nX = gn[0][lx];
+        nY = gn[1][ly];
+        nZ = gn[2][lz];
+        lists = nX >= 0 && nY >= 0 && nZ >= 0;
+        if (lists) tot = nX * nY * nZ;
+    }
+#pragma unroll
+    for (int u = 0; u < SMAX; ++u) {
+        const int k = w + GSUB * u;
+        sv[u][0] = sv[u][1] = sv[u][2] = 0.0f;
+        if (k < tot) {
+            const int jx = k % nX, r = k / nX;
+            const int jy = r % nY, jz = r / nY;
+            const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
+            sv[u][0] = p[0];
+            sv[u][1] = p[1];
+            sv[u][2] = p[2];
+        }
+    }
     if (a.has_penalty) {
         constexpr int NH = GPX * GPY * GPZ;
         constexpr int KP = (NH + GT3 - 1) / GT3;
@@ -855,32 +881,6 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     }
     __syncthreads();
 
-    // batch 2: this warp's share of the partial slots (entries k = w,
-    // w + 8, ...) of the lane's coefficient, issued before the stencil
-    constexpr int SMAX = GSMAX;
-    float sv[SMAX][3];
-    int tot = 0, nX = 0, nY = 0, nZ = 0;
-    bool lists = false;
-    if (valid && img) {
-        nX = gn[0][lx];
-        nY = gn[1][ly];
-        nZ = gn[2][lz];
-        lists = nX >= 0 && nY >= 0 && nZ >= 0;
-        if (lists) tot = nX * nY * nZ;
-    }
-#pragma unroll
-    for (int u = 0; u < SMAX; ++u) {
-        const int k = w + GSUB * u;
-        sv[u][0] = sv[u][1] = sv[u][2] = 0.0f;
-        if (k < tot) {
-            const int jx = k % nX, r = k / nX;
-            const int jy = r % nY, jz = r / nY;
-            const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
-            sv[u][0] = p[0];
-            sv[u][1] = p[1];
-            sv[u][2] = p[2];
-        }
-    }
     // R0..R5, T0..T2: the nine products of the 3x3 cell with c_j, summed
     // over the 7^3 neighbours j = i - d (zero outside the grid)
     float R0 = 0, R1 = 0, R2 = 0, R3 = 0, R4 = 0, R5 = 0, T0 = 0, T1 = 0, T2 = 0;
