@@ -88,9 +88,12 @@ __device__ __forceinline__ void pdl_trigger()
 // ---------------------------------------------------------------------
 // warp
 // ---------------------------------------------------------------------
-template <int TZ>
+// COST: the image cost when known at compile time (MGR_COST_SSD / NCC; the
+// one-pair kernels are compiled per cost), -1 to read it from a
+template <int TZ, int COST>
 __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, int bz, int ntiles, int tile)
 {
+    const int cost = COST >= 0 ? COST : a.cost;
     extern __shared__ __align__(16) float sm3[];
     __shared__ double red[5 * (NT3 / 32)];
     __shared__ float wsum[5][NT3 / 32];
@@ -382,7 +385,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         return 0.0f;
     };
     auto add_cost = [&](float wv, float b) {
-        if (a.cost == 0) {
+        if (cost == 0) {
             const float d = wv - b;
             acc[0] += d * d;
         } else {
@@ -508,7 +511,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     // tile sums: a float tree within each warp (5 levels), the warps' sums
     // added in double in a fixed order by thread 0 (FP64 is slow here, so
     // it is kept off the per-thread path)
-    const int ncomp = a.cost == 0 ? 1 : 5;
+    const int ncomp = cost == 0 ? 1 : 5;
 #pragma unroll
     for (int k = 0; k < 5; ++k)
         if (k < ncomp) {
@@ -542,6 +545,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
 template <int TZ, int UNROLL>
 __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by, int bz, int tile_index)
 {
+    const int cost = a.cost;   // (a per-cost NCC kernel spills under the register cap)
     extern __shared__ __align__(16) float sm3[];
     __shared__ int asx[TX3], asy[TY3], azs[TZ];
     __shared__ float fsc[5];   // force constants (converted once per block)
@@ -619,7 +623,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
             g[1] = by_in ? 0.5f * (yp - ym) : 0.0f;
             g[2] = (z > 0 && z < nz - 1) ? 0.5f * (wp - wm) : 0.0f;
             const float b = __ldg(rc);
-            if (a.cost == 0) {
+            if (cost == 0) {
                 const float d = w0 - b;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) f[k] = (g[k] * d) * fscale;
@@ -1050,11 +1054,11 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
 #define MGR_WARP_MINB 3
 #endif
 
-template <int TZ>
+template <int TZ, int COST>
 __global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3(const __grid_constant__ EvalArgs a)
 {
     const int tile = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    warp3_body<TZ>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, tile);
+    warp3_body<TZ, COST>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, tile);
 }
 
 template <int TZ>
@@ -1088,7 +1092,7 @@ __global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3_batch(const EvalAr
     const EvalArgs &a = args[it.x];
     int bx, by, bz, nt;
     decode_tile3(a, it.y, bx, by, bz, nt);
-    warp3_body<TZ>(a, bx, by, bz, nt, it.y);
+    warp3_body<TZ, -1>(a, bx, by, bz, nt, it.y);
 }
 
 template <int TZ>
@@ -1143,7 +1147,7 @@ __global__ void __launch_bounds__(NT3, MGR_WARP_MINB) k_warp3_queue(const EvalAr
         const EvalArgs &a = args[it.x];
         int bx, by, bz, nt;
         decode_tile3(a, it.y, bx, by, bz, nt);
-        warp3_body<TZ>(a, bx, by, bz, nt, it.y);
+        warp3_body<TZ, -1>(a, bx, by, bz, nt, it.y);
     }
     queue_done(queue);
 }
@@ -1255,11 +1259,19 @@ bool tile_supported3(int tx, int ty, int tz)
 
 namespace {
 
+template <int TZ, int COST>
+void launch_warp3_zc(const EvalArgs &a, size_t sm, cudaStream_t st)
+{
+    cudaFuncSetAttribute(k_warp3<TZ, COST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    launch_pdl(a.pdl != 0, k_warp3<TZ, COST>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
+}
 template <int TZ>
 void launch_warp3_z(const EvalArgs &a, size_t sm, cudaStream_t st)
 {
-    cudaFuncSetAttribute(k_warp3<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-    launch_pdl(a.pdl != 0, k_warp3<TZ>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
+    if (a.cost == MGR_COST_SSD)
+        launch_warp3_zc<TZ, MGR_COST_SSD>(a, sm, st);
+    else
+        launch_warp3_zc<TZ, MGR_COST_NCC>(a, sm, st);
 }
 
 template <int TZ>
