@@ -282,7 +282,10 @@ constexpr int GATHER_LMAX = 24;
 // tile-fit rule (mgr_level::tile_fits) counts them.  12 keeps three warp
 // blocks per SM at the usual spacings (14 measured slower: 2 blocks per SM
 // at rate 5)
-constexpr int WARP_RING_PLANES = 12;
+#ifndef MGR_RING_PLANES
+#define MGR_RING_PLANES 12
+#endif
+constexpr int WARP_RING_PLANES = MGR_RING_PLANES;
 
 // scalars written by the cost finalisation (double[16])
 enum {
