@@ -825,36 +825,13 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             }
         }
     }
-    __syncthreads();   // the offset lists
-    pdl_wait();
-    pdl_trigger();
-    // this warp's share of the partial slots (entries k = w, w + GSUB, ...)
-    // of the lane's coefficient and the parameters with their halo: one
-    // batch of independent loads, issued before the stencil
-    constexpr int SMAX = GSMAX;
-    float sv[SMAX][3];
-    int tot = 0, nX = 0, nY = 0, nZ = 0;
-    bool lists = false;
-    if (valid && img) {
-        nX = gn[0][lx];
-        nY = gn[1][ly];
-        nZ = gn[2][lz];
-        lists = nX >= 0 && nY >= 0 && nZ >= 0;
-        if (lists) tot = nX * nY * nZ;
-    }
-#pragma unroll
-    for (int u = 0; u < SMAX; ++u) {
-        const int k = w + GSUB * u;
-        sv[u][0] = sv[u][1] = sv[u][2] = 0.0f;
-        if (k < tot) {
-            const int jx = k % nX, r = k / nX;
-            const int jy = r % nY, jz = r / nY;
-            const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
-            sv[u][0] = p[0];
-            sv[u][1] = p[1];
-            sv[u][2] = p[2];
-        }
-    }
+    // The divcurl stencil needs only the parameters' float copy, which
+    // every launch order of this kernel has completed before any block of
+    // it starts (the conversion kernel is never launched directly before
+    // it; the kernel between them waits for the conversion before it lets
+    // this one launch).  So the stencil runs before the dependency wait,
+    // while the adjoint kernel finishes; the copy is read through the L2
+    // (ld.global.cg), never from a line an earlier kernel left in L1.
     if (a.has_penalty) {
         constexpr int NH = GPX * GPY * GPZ;
         constexpr int KP = (NH + GT3 - 1) / GT3;
@@ -868,9 +845,9 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 const int gx = cx0 - GH + hx, gy = cy0 - GH + hy, gz = cz0 - GH + hz;
                 if (gx >= 0 && gx < ncx && gy >= 0 && gy < ncy && gz >= 0 && gz < ncz) {
                     const float *p = a.params_f + ((size_t(gz) * ncy + gy) * ncx + gx) * 3;
-                    pv[k][0] = p[0];
-                    pv[k][1] = p[1];
-                    pv[k][2] = p[2];
+                    pv[k][0] = __ldcg(p);
+                    pv[k][1] = __ldcg(p + 1);
+                    pv[k][2] = __ldcg(p + 2);
                 }
             }
         }
@@ -883,8 +860,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
             }
         }
     }
-    __syncthreads();
-
+    __syncthreads();   // the offset lists, the parameter halo
     // R0..R5, T0..T2: the nine products of the 3x3 cell with c_j, summed
     // over the 7^3 neighbours j = i - d (zero outside the grid)
     float R0 = 0, R1 = 0, R2 = 0, R3 = 0, R4 = 0, R5 = 0, T0 = 0, T1 = 0, T2 = 0;
@@ -907,6 +883,34 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 T1 += t0.y * cj.x;
                 T2 += t0.w * cj.y;
             }
+        }
+    }
+    pdl_wait();
+    pdl_trigger();
+    // the adjoint's partial slots: this warp's share (entries k = w,
+    // w + GSUB, ...) of the lane's coefficient, one batch of loads
+    constexpr int SMAX = GSMAX;
+    float sv[SMAX][3];
+    int tot = 0, nX = 0, nY = 0, nZ = 0;
+    bool lists = false;
+    if (valid && img) {
+        nX = gn[0][lx];
+        nY = gn[1][ly];
+        nZ = gn[2][lz];
+        lists = nX >= 0 && nY >= 0 && nZ >= 0;
+        if (lists) tot = nX * nY * nZ;
+    }
+#pragma unroll
+    for (int u = 0; u < SMAX; ++u) {
+        const int k = w + GSUB * u;
+        sv[u][0] = sv[u][1] = sv[u][2] = 0.0f;
+        if (k < tot) {
+            const int jx = k % nX, r = k / nX;
+            const int jy = r % nY, jz = r / nY;
+            const float *p = a.partial + (size_t(gl[2][lz][jz] + gl[1][ly][jy]) + gl[0][lx][jx]);
+            sv[u][0] = p[0];
+            sv[u][1] = p[1];
+            sv[u][2] = p[2];
         }
     }
     float S0 = 0.0f, S1 = 0.0f, S2 = 0.0f;
