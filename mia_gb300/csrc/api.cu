@@ -60,6 +60,29 @@ cudaError_t host_malloc_pinned(void **p, size_t bytes)
     return cudaMallocHost(p, bytes);
 }
 
+void raise_smem_limit(const void *kernel, size_t bytes)
+{
+    struct Limit {
+        const void *kernel;
+        int device;
+        size_t bytes;
+    };
+    static std::mutex mu;
+    static std::vector<Limit> set;
+    int device = 0;
+    cudaGetDevice(&device);
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto &l : set)
+        if (l.kernel == kernel && l.device == device) {
+            if (l.bytes >= bytes) return;
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+            l.bytes = bytes;
+            return;
+        }
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+    set.push_back({kernel, device, bytes});
+}
+
 // phase trace (MGR_TRACE=1)
 namespace {
 struct PhaseSum {

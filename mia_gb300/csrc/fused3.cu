@@ -515,7 +515,7 @@ namespace {
 template <int TZ>
 void launch_fused3_z(const EvalArgs &a, int with_gradient, size_t sm, cudaStream_t st)
 {
-    cudaFuncSetAttribute(k_fused3<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    raise_smem_limit(reinterpret_cast<const void *>(k_fused3<TZ>), sm);
     k_fused3<TZ><<<dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), NTF, sm, st>>>(a, with_gradient);
 }
 }  // namespace

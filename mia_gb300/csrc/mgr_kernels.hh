@@ -27,6 +27,12 @@ cudaError_t dev_malloc_async(void **p, size_t bytes, cudaStream_t s);
 cudaError_t dev_malloc(void **p, size_t bytes);
 cudaError_t host_malloc_pinned(void **p, size_t bytes);
 
+// cudaFuncSetAttribute(kernel, MaxDynamicSharedMemorySize, bytes) on the
+// current device, made only when `bytes` exceeds what was set for that
+// kernel and device before (the limit only grows): a launch of an
+// evaluation then makes no driver call for it
+void raise_smem_limit(const void *kernel, size_t bytes);
+
 void launch_prefilter(float *img, int dim, int nx, int ny, int nz, cudaStream_t st);
 // padded copy with the mirror fold applied in the halo (layout of coef_pad)
 void launch_pad_mirror(const float *img, float *pad, int dim, int nx, int ny, int nz, cudaStream_t st);

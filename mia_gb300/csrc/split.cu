@@ -549,11 +549,11 @@ static void launch_tile(const EvalArgs &a, int which, cudaStream_t st)
 {
     if (which == 0) {
         const size_t sm = warp_smem(a);
-        cudaFuncSetAttribute(k_warp_t<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        raise_smem_limit(reinterpret_cast<const void *>(k_warp_t<D, TX, TY, TZ>), sm);
         k_warp_t<D, TX, TY, TZ><<<tile_grid(a), NT, sm, st>>>(a);
     } else {
         const size_t sm = adjoint_smem(a);
-        cudaFuncSetAttribute(k_adjoint_t<D, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        raise_smem_limit(reinterpret_cast<const void *>(k_adjoint_t<D, TX, TY, TZ>), sm);
         k_adjoint_t<D, TX, TY, TZ><<<tile_grid(a), NT, sm, st>>>(a);
     }
     count_launch();

@@ -1266,7 +1266,7 @@ namespace {
 template <int TZ, int COST>
 void launch_warp3_zc(const EvalArgs &a, size_t sm, cudaStream_t st)
 {
-    cudaFuncSetAttribute(k_warp3<TZ, COST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    raise_smem_limit(reinterpret_cast<const void *>(k_warp3<TZ, COST>), sm);
     launch_pdl(a.pdl != 0, k_warp3<TZ, COST>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
 }
 template <int TZ>
@@ -1281,7 +1281,7 @@ void launch_warp3_z(const EvalArgs &a, size_t sm, cudaStream_t st)
 template <int TZ>
 void launch_adjoint3_z(const EvalArgs &a, size_t sm, cudaStream_t st)
 {
-    cudaFuncSetAttribute(k_adjoint3<TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    raise_smem_limit(reinterpret_cast<const void *>(k_adjoint3<TZ>), sm);
     launch_pdl(a.pdl != 0, k_adjoint3<TZ>, dim3(a.ax[0].nt, a.ax[1].nt, a.ax[2].nt), dim3(NT3), sm, st, a);
 }
 
