@@ -980,6 +980,10 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     __syncthreads();
     if (w == 0) {
         float pval = 0.0f;
+        // parameters the conversion found non-finite: nothing is written to
+        // the caller's buffers (uniform over the block)
+        const bool bad = a.params_host && *(volatile unsigned *)&a.counters[7] != 0u;
+        double gt[3] = {0.0, 0.0, 0.0};
         if (valid) {
             float v9[GNQ];
 #pragma unroll
@@ -996,18 +1000,51 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
                 gp[1] = pw * (v9[7] + (2.0f * v9[2] + v9[3]));
                 gp[2] = pw * (v9[8] + (2.0f * v9[4] + v9[5]));
             }
-            // parameters the conversion found non-finite: nothing is written
-            // to the caller's buffers
-            const bool bad = a.params_host && *(volatile unsigned *)&a.counters[7] != 0u;
             if (with_gradient && !bad) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const double gi = image_from_dense ? a.grad_image[i * 3 + k] : double(cw * -v9[9 + k]);
-                    a.grad_total[i * 3 + k] = gi + double(gp[k]);
+                    gt[k] = gi + double(gp[k]);
                     if (a.grad_image && !image_from_dense) a.grad_image[i * 3 + k] = gi;
                     if (a.grad_penalty) a.grad_penalty[i * 3 + k] = double(gp[k]);
                 }
             }
+        }
+        if (with_gradient && !bad && !a.params_host) {
+            if (valid)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a.grad_total[i * 3 + k] = gt[k];
+        } else if (with_gradient && !bad) {
+            // the total gradient into the caller's host memory: the lanes of
+            // a row (ly, lz) hold four consecutive coefficients, 96
+            // contiguous bytes of the output; a row whose four coefficients
+            // are all in the grid and whose start is 16-byte aligned is
+            // stored as six 16-byte pieces (few large writes over the
+            // CPU-GPU link: an evaluation from host buffers took 153.9
+            // instead of 158.0 us at 192x192x128), any other lane stores
+            // its own three values
+            __shared__ __align__(16) double gst[32 * 3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gst[lane * 3 + k] = gt[k];
+            __syncwarp();
+            auto row_dst = [&](int r) -> double * {
+                const int ry = cy0 + (r & 3), rz = cz0 + (r >> 2);
+                return a.grad_total + ((size_t(rz) * ncy + ry) * ncx + cx0) * 3;
+            };
+            auto row_vec = [&](int r) -> bool {
+                const int ry = cy0 + (r & 3), rz = cz0 + (r >> 2);
+                return cx0 + GBX <= ncx && ry < ncy && rz < ncz &&
+                       (reinterpret_cast<uintptr_t>(row_dst(r)) & 15u) == 0;
+            };
+            for (int c = lane; c < 48; c += 32) {
+                const int r = c / 6, piece = c - r * 6;
+                if (row_vec(r))
+                    reinterpret_cast<double2 *>(row_dst(r))[piece] =
+                        *reinterpret_cast<const double2 *>(&gst[r * 12 + piece * 2]);
+            }
+            if (valid && !row_vec(lane >> 2))
+#pragma unroll
+                for (int k = 0; k < 3; ++k) a.grad_total[i * 3 + k] = gt[k];
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) pval += __shfl_xor_sync(FULL, pval, o);
