@@ -124,6 +124,17 @@ def profile_traffic(kernel):
     return None
 
 
+def profile_metric(kernel, key):
+    """a per-launch figure of `kernel` from the committed ncu summary"""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            v = json.load(f).get(kernel)
+        if v and key in v:
+            return float(v[key])
+    return None
+
+
 def cpu_baseline(w, mov, ref, params, seconds, threads):
     from oracle import oracle as O
     size = w["size"]
@@ -677,6 +688,19 @@ def run_gpu(args):
             "charged": "B_eval = 8 N + 12 d C bytes of the whole evaluation over the dominant kernel's time"}
     eval_roof = {"achieved": b_eval / t_step / 1e9, "frac": b_eval / t_step / 1e9 / peak,
                  "algorithmic_bytes": b_eval, "unit": "GB/s", "traffic": profile_traffic("evaluation")}
+    clocks = clk.summary()
+    # the bound that limits k_warp3 in practice: its shared-memory data path
+    # (one 128-byte wavefront per SM and clock); wavefronts per launch from
+    # the committed ncu capture of this workload, time from this run
+    wf = profile_metric("k_warp3", "shared_wavefronts") if name == "3d_ssd_192x192x128" else None
+    smem_roof = None
+    if wf and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_smem = sms * 128.0 * clocks["sm_mhz"] * 1e6 / 1e12
+        ach = wf * 128.0 / (kms["k_warp3"] / 1e3) / 1e12
+        smem_roof = {"kernel": "k_warp3", "bound": "shared memory (L1/shared data path)", "achieved": ach,
+                     "peak": peak_smem, "unit": "TB/s", "frac": ach / peak_smem,
+                     "wavefronts_per_launch": wf, "peak_rule": "SMs x 128 B x median SM clock of this run"}
     line = {
         "metric": METRIC, "value": value, "unit": "Mvoxel/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -693,7 +717,8 @@ def run_gpu(args):
         "kernel_ms": {"warp": kms["k_warp3"], "adjoint": kms["k_adjoint3"], "gather_penalty": kms["k_gather3"]},
         "roofline": roof,
         "eval_roofline": eval_roof,
-        "clocks": clk.summary(),
+        "shared_memory_roofline": smem_roof,
+        "clocks": clocks,
     }
     if ws == 1:
         line["split_vs_plain"] = split_vs_plain(lv, p_d, g_d, c_d, flush, max(3, min(args.steps, 10)), N)
