@@ -279,7 +279,7 @@ struct mgr_level {
         build_axis(hz, n[2], nc[2], t[2]);
         const size_t w =
             (size_t(3) * hz.fc * hy.fc * (hx.fc + 32) + 32 + size_t(WARP_RING_PLANES) * 16 * 64) * sizeof(float);
-        const size_t adj = size_t(3) * hz.ac * (8 * 32 + hy.ac * 33) * sizeof(float);
+        const size_t adj = size_t(3) * hz.ac * 8 * (33 + hx.ac) * sizeof(float);   // split3_smem(a, 1)
         if (strict) return w <= 74 * 1024 && adj <= 64 * 1024;
         return w + 128 <= 200 * 1024 && adj <= 200 * 1024;
     }

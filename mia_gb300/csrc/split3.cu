@@ -25,10 +25,11 @@
 //       neighbours carried in registers; mia/3d/image.cc:347-466), the SSD /
 //       NCC force (mia/template/ssd.hh:126-181, mia/3d/cost/ncc.cc:88-128),
 //       and the transposed spline contraction (translate,
-//       spline.cc:731-791) in the reference's order: z while walking (four
-//       running sums per component, the lowest one final when the window
-//       moves on), then y and x in shared memory; the result goes to the
-//       tile's partial slot (no atomics).
+//       spline.cc:731-791): z while walking (four running sums per
+//       component, the lowest one final when the window moves on), then x
+//       and y in shared memory (the reference contracts y before x; the
+//       order changes only the rounding, and x first keeps the intermediate
+//       small); the result goes to the tile's partial slot (no atomics).
 //   k_gather3         per 4x4x4 block of coefficients: the fixed-order sum of
 //       the partial slots that hold each coefficient, the divcurl stencil
 //       (C3DPPDivcurlMatrixImpl::evaluate / multiply,
@@ -558,9 +559,9 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
     const int ax0 = X.atile0[bx], ay0 = Y.atile0[by], az0 = Z.atile0[bz];
     const int tid = threadIdx.x, lane = tid & 31, wy = tid >> 5;
     float *part = a.partial + size_t(tile_index) * a.slot;
-    constexpr int AYP = TX3 + 1;              // Ay row pitch (odd: the x stage reads columns)
-    float *Az = sm3;                          // [3][AZc][8][32]
-    float *Ay = Az + 3 * AZc * TY3 * TX3;     // [3][AZc][AYc][AYP]
+    constexpr int AZP = TX3 + 1;              // Az row pitch (odd: the x stage reads along the rows)
+    float *Az = sm3;                          // [3][AZc][8][AZP]
+    float *Ax = Az + 3 * AZc * TY3 * AZP;     // [3][AZc][8][AXc]
 
     // tables, scalars and the first planes of the column, loaded up front
     const int x = x0 + lane, y = y0 + wy;
@@ -607,7 +608,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
 #pragma unroll
         for (int k = 0; k < 4; ++k) acc[c][k] = 0.0f;
     int cur = 0;   // azs[0] == 0
-    auto emit = [&](int kz, int c, float v) { Az[((c * AZc + kz) * TY3 + wy) * TX3 + lane] = v; };
+    auto emit = [&](int kz, int c, float v) { Az[((c * AZc + kz) * TY3 + wy) * AZP + lane] = v; };
 #pragma unroll UNROLL
     for (int t = 0; t < ez; ++t) {
         const int z = z0 + t;
@@ -667,53 +668,22 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
 #pragma unroll
         for (int c = 0; c < 3; ++c) emit(kz, c, 0.0f);
     __syncthreads();
-    // y stage, one thread per (c, kz, lane) column of Az: the transposed
-    // contraction over the tile's rows as a sliding window of four sums
-    // (the row starts are the same for every thread, so the window moves in
-    // lock step); Ay rows have an odd pitch for the x stage
-    for (int e = tid; e < 3 * AZc * TX3; e += NT3) {
-        const int l = e & (TX3 - 1), ck = e >> 5;
-        const float *src = Az + ck * TY3 * TX3 + l;
-        float *dst = Ay + ck * AYc * AYP + l;
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-        int oc = 0;
-        for (int yy = 0; yy < ey; ++yy) {
-            const int o = asy[yy];
-            while (oc < o) {
-                dst[oc * AYP] = s0;
-                s0 = s1;
-                s1 = s2;
-                s2 = s3;
-                s3 = 0.0f;
-                ++oc;
-            }
-            const float4 w = awy[yy];
-            const float f = src[yy * TX3];
-            s0 += w.x * f;
-            s1 += w.y * f;
-            s2 += w.z * f;
-            s3 += w.w * f;
-        }
-        if (oc < AYc) dst[oc * AYP] = s0;
-        if (oc + 1 < AYc) dst[(oc + 1) * AYP] = s1;
-        if (oc + 2 < AYc) dst[(oc + 2) * AYP] = s2;
-        if (oc + 3 < AYc) dst[(oc + 3) * AYP] = s3;
-        for (int jy = oc + 4; jy < AYc; ++jy) dst[jy * AYP] = 0.0f;
-    }
-    __syncthreads();
-    // x stage, one thread per (c, kz, jy) row of Ay, the same sliding window
-    // over the lanes, straight into the partial slot
-    // ((kz AYc + jy) AXc + ix) 3 + c
-    for (int e = tid; e < 3 * AZc * AYc; e += NT3) {
-        const int c = e / (AZc * AYc), kzjy = e - c * (AZc * AYc);
-        const float *src = Ay + (c * AZc * AYc + kzjy) * AYP;
-        float *dst = part + size_t(kzjy) * AXc * 3 + c;
+    // x stage, one thread per (c, kz, row) row of Az: the transposed
+    // contraction over the tile's columns as a sliding window of four sums
+    // (the column starts are the same for every thread, so the window moves
+    // in lock step).  Contracting x before y keeps the intermediate small
+    // (AXc instead of 32 values per row): the block needs less shared
+    // memory and the two stages fewer instructions.
+    for (int e = tid; e < 3 * AZc * TY3; e += NT3) {
+        if ((e & (TY3 - 1)) >= ey) continue;   // rows below the image: never read
+        const float *src = Az + e * AZP;
+        float *dst = Ax + e * AXc;
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
         int oc = 0;
         for (int l = 0; l < ex; ++l) {
             const int o = asx[l];
             while (oc < o) {
-                dst[oc * 3] = s0;
+                dst[oc] = s0;
                 s0 = s1;
                 s1 = s2;
                 s2 = s3;
@@ -727,11 +697,46 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
             s2 += w.z * f;
             s3 += w.w * f;
         }
-        if (oc < AXc) dst[oc * 3] = s0;
-        if (oc + 1 < AXc) dst[(oc + 1) * 3] = s1;
-        if (oc + 2 < AXc) dst[(oc + 2) * 3] = s2;
-        if (oc + 3 < AXc) dst[(oc + 3) * 3] = s3;
-        for (int ix = oc + 4; ix < AXc; ++ix) dst[ix * 3] = 0.0f;
+        if (oc < AXc) dst[oc] = s0;
+        if (oc + 1 < AXc) dst[oc + 1] = s1;
+        if (oc + 2 < AXc) dst[oc + 2] = s2;
+        if (oc + 3 < AXc) dst[oc + 3] = s3;
+        for (int ix = oc + 4; ix < AXc; ++ix) dst[ix] = 0.0f;
+    }
+    __syncthreads();
+    // y stage, one thread per (c, kz, ix) column of Ax, the same sliding
+    // window over the rows, straight into the partial slot
+    // ((kz AYc + jy) AXc + ix) 3 + c
+    for (int e = tid; e < 3 * AZc * AXc; e += NT3) {
+        const int c = e / (AZc * AXc), r = e - c * (AZc * AXc);
+        const int kz = r / AXc, ix = r - kz * AXc;
+        const float *src = Ax + (c * AZc + kz) * TY3 * AXc + ix;
+        float *dst = part + (size_t(kz) * AYc * AXc + ix) * 3 + c;
+        const int pitch = AXc * 3;
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        int oc = 0;
+        for (int yy = 0; yy < ey; ++yy) {
+            const int o = asy[yy];
+            while (oc < o) {
+                dst[oc * pitch] = s0;
+                s0 = s1;
+                s1 = s2;
+                s2 = s3;
+                s3 = 0.0f;
+                ++oc;
+            }
+            const float4 w = awy[yy];
+            const float f = src[yy * AXc];
+            s0 += w.x * f;
+            s1 += w.y * f;
+            s2 += w.z * f;
+            s3 += w.w * f;
+        }
+        if (oc < AYc) dst[oc * pitch] = s0;
+        if (oc + 1 < AYc) dst[(oc + 1) * pitch] = s1;
+        if (oc + 2 < AYc) dst[(oc + 2) * pitch] = s2;
+        if (oc + 3 < AYc) dst[(oc + 3) * pitch] = s3;
+        for (int jy = oc + 4; jy < AYc; ++jy) dst[jy * pitch] = 0.0f;
     }
 }
 
@@ -1290,7 +1295,7 @@ size_t split3_smem(const EvalArgs &a, int which)
     if (which == 0)
         return size_t(3) * Z.fc * Y.fc * (X.fc + TX3) * sizeof(float) + 128 +
                size_t(RING_N) * RING_PLANE * sizeof(float);
-    return size_t(3) * Z.ac * (TY3 * TX3 + Y.ac * (TX3 + 1)) * sizeof(float);
+    return size_t(3) * Z.ac * TY3 * (TX3 + 1 + X.ac) * sizeof(float);
 }
 
 bool tile_supported3(int tx, int ty, int tz)
