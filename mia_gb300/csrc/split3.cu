@@ -275,7 +275,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     // needs t .. t + span - 1; the ring is filled by bulk copies, one per
     // row, completion counted on the plane's mbarrier
     constexpr int H = PAD_H;
-    auto issue_plane = [&](int k) {   // thread 0: plane k of the box into its ring slot, one tensor copy
+    auto issue_plane = [&](int k) {   // one thread: plane k of the box into its ring slot, one tensor copy
         const int slot = ring_slot(k);
         const unsigned mb = smem_u32(&mbar[slot]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb),
@@ -331,14 +331,13 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         boxs[5] = dzh - dzl + 1;
         boxs[6] = RING_X;
         boxs[7] = yhi - ylo + 1;
-        nissued = 0;
         ring_failed = 0;
-        if (ok) {
-            for (int k = 0; k < min(boxs[4], RING_N); ++k) issue_plane(k);
-            nissued = min(boxs[4], RING_N);
-        }
+        nissued = ok ? min(boxs[4], RING_N) : 0;
     }
     __syncthreads();
+    // the box's first planes, one tensor copy per lane of warp 0 (the
+    // walk's waits on a plane end once its copy has been issued and landed)
+    if (wy == 0 && lane < nissued) issue_plane(lane);
 
     const bool inxy = (x0 + lane < nx) && (y0 + wy < ny);
     const float px0 = float(x0 + lane), py0 = float(y0 + wy);
