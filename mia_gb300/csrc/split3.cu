@@ -196,11 +196,9 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             const float *c = C + r * FX + sx;
             Tx[r * 32 + lane] = fwx.x * c[0] + fwx.y * c[1] + fwx.z * c[2] + fwx.w * c[3];
         }
-        if (tid == 0) {
-            for (int k = 0; k < RING_N; ++k) {
-                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[k])) : "memory");
-                rdone[k] = 0;
-            }
+        if (tid < RING_N) {   // one ring slot per lane of warp 0
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[tid])) : "memory");
+            rdone[tid] = 0;
             asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         }
     }
@@ -288,17 +286,22 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             "r"(mb)
             : "memory");
     };
-    if (tid == 0) {
-        float ulo[3], uhi[3];
+    // the displacement range of the tile: lane k < 6 of warp 0 reduces bound
+    // k over the warps (lanes 0-2 the minima, 3-5 the maxima), lane 0 then
+    // sets the box
+    float urange = 0.0f;
+    if (wy == 0 && lane < 6) {
+        urange = urng[0][lane];
+        for (int w = 1; w < NT3 / 32; ++w)
+            urange = lane < 3 ? fminf(urange, urng[w][lane]) : fmaxf(urange, urng[w][lane]);
+    }
+    float ulo[3], uhi[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            ulo[c] = urng[0][c];
-            uhi[c] = urng[0][3 + c];
-            for (int w = 1; w < NT3 / 32; ++w) {
-                ulo[c] = fminf(ulo[c], urng[w][c]);
-                uhi[c] = fmaxf(uhi[c], urng[w][3 + c]);
-            }
-        }
+    for (int c = 0; c < 3; ++c) {
+        ulo[c] = __shfl_sync(FULL, urange, c);
+        uhi[c] = __shfl_sync(FULL, urange, 3 + c);
+    }
+    if (tid == 0) {
         // taps of a voxel at p = v - u: floor(p) - 1 .. floor(p) + 2; the
         // fixed-point floor may round p up to the next integer, one more
         // row / column / plane on the upper side
