@@ -550,6 +550,8 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         return;
     }
     L->record(0);
+    // 3D SSD: the gather finalises the cost (the warp kernel ends earlier)
+    a.defer_cost = L->d.dim == 3 && L->d.cost == MGR_COST_SSD;
     {
         NvtxRange r(L->d.dim == 3 ? "k_warp3" : "k_warp (2D)");
         launch_warp(a, st);
@@ -667,6 +669,7 @@ mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_im
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
         upload_params(lvl, params);
         EvalArgs a = lvl->args();
+        a.defer_cost = lvl->d.dim == 3 && lvl->d.cost == MGR_COST_SSD;   // the gather finalises the cost
         launch_warp(a, lvl->stream);
         launch_gather(a, 0, lvl->stream);
         check_launch("value kernels");

@@ -95,6 +95,11 @@ struct EvalArgs {
     // to host_out; the gradient pointers above may then be host memory too
     const double *params_host;
     double *host_out;
+    // 1: an SSD cost is finalised by the gather's last block from the warp
+    // kernel's tile sums (the warp kernel then ends without a device-wide
+    // fence and last-block reduction, and the adjoint takes its force scale
+    // from the settings); 0: the warp kernel finalises the cost
+    int defer_cost;
     // 1: the 3D split path's warp, adjoint and gather kernels are launched
     // with programmatic stream serialisation (each may start while the one
     // before it finishes, and waits for it before reading its outputs)

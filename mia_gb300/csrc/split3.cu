@@ -523,6 +523,8 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             if (lane == 0) wsum[k][wy] = acc[k];
         }
     __syncthreads();
+    // an SSD cost the gather finalises needs no last-block pass here
+    const bool finalise_here = !(a.defer_cost && cost == 0);
     if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
@@ -531,8 +533,11 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
                 for (int w = 0; w < NT3 / 32; ++w) v += double(wsum[k][w]);
             a.tile_sums[size_t(tile) * 5 + k] = v;
         }
-        __threadfence();
-        is_last = (atomicAdd(&a.counters[0], 1u) == unsigned(ntiles - 1));
+        is_last = false;
+        if (finalise_here) {
+            __threadfence();
+            is_last = (atomicAdd(&a.counters[0], 1u) == unsigned(ntiles - 1));
+        }
     }
     __syncthreads();
     if (is_last) {
@@ -598,6 +603,9 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
     if (tid < 5) {
         const int slot[5] = {SC_K1, SC_K2, SC_MA, SC_MB, SC_FSCALE};
         fsc[tid] = float(a.scalars[slot[tid]]);
+        // the SSD force scale from the settings, as the finalisation sets it
+        // (with a deferred finalisation it is not set yet)
+        if (tid == 4 && cost == 0) fsc[4] = a.ssd_norm ? float(1.0 / double(size_t(nx) * ny * nz)) : 1.0f;
     }
     float wm = (z0 > 0) ? __ldg(wc - nxy) : 0.0f;
     float w0 = __ldg(wc);
@@ -1064,9 +1072,22 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     __syncthreads();
     if (is_last) {
         __threadfence();
+        __shared__ double red[GT3 / 32];
+        if (a.defer_cost) {
+            // the SSD cost from the warp kernel's tile sums: the fixed-order
+            // reduction of reduce_tile_sums (same striding, one component)
+            const int ntw = a.ax[0].nt * a.ax[1].nt * a.ax[2].nt;
+            double tv[1] = {0.0};
+            for (int t = tid; t < ntw; t += GT3) tv[0] += ((volatile double *)a.tile_sums)[size_t(t) * 5];
+            block_sum<1>(tv, red);
+            if (tid == 0) {
+                const double s5[5] = {tv[0], 0.0, 0.0, 0.0, 0.0};
+                finalise_cost(a, s5, size_t(a.n[0]) * a.n[1] * a.n[2]);
+            }
+            __syncthreads();
+        }
         double sv1[1] = {0.0};
         for (unsigned b = tid; b < unsigned(nblk); b += GT3) sv1[0] += ((volatile double *)a.pen_part)[b];
-        __shared__ double red[GT3 / 32];
         block_sum<1>(sv1, red);
         if (tid == 0) {
             double *sc = a.scalars;
