@@ -550,8 +550,8 @@ static void run_image_term(mgr_level *L, EvalArgs &a, bool with_gradient)
         return;
     }
     L->record(0);
-    // 3D SSD: the gather finalises the cost (the warp kernel ends earlier)
-    a.defer_cost = L->d.dim == 3 && L->d.cost == MGR_COST_SSD;
+    // 3D: the cost is finalised after the warp kernel (its blocks end earlier)
+    a.defer_cost = L->d.dim == 3;
     {
         NvtxRange r(L->d.dim == 3 ? "k_warp3" : "k_warp (2D)");
         launch_warp(a, st);
@@ -669,7 +669,7 @@ mgr_status mgr_level_value(mgr_level *lvl, const double *params, double *cost_im
         ck(cudaSetDevice(lvl->device), "cudaSetDevice");
         upload_params(lvl, params);
         EvalArgs a = lvl->args();
-        a.defer_cost = lvl->d.dim == 3 && lvl->d.cost == MGR_COST_SSD;   // the gather finalises the cost
+        a.defer_cost = lvl->d.dim == 3;   // the cost is finalised after the warp kernel
         launch_warp(a, lvl->stream);
         launch_gather(a, 0, lvl->stream);
         check_launch("value kernels");

@@ -95,10 +95,12 @@ struct EvalArgs {
     // to host_out; the gradient pointers above may then be host memory too
     const double *params_host;
     double *host_out;
-    // 1: an SSD cost is finalised by the gather's last block from the warp
-    // kernel's tile sums (the warp kernel then ends without a device-wide
-    // fence and last-block reduction, and the adjoint takes its force scale
-    // from the settings); 0: the warp kernel finalises the cost
+    // 1: the cost is finalised after the warp kernel from its tile sums
+    // (the warp blocks then end without a device-wide fence and last-block
+    // reduction): an SSD cost by the gather's last block (the adjoint takes
+    // its force scale from the settings), an NCC cost by k_finalise3, which
+    // launch_warp3 queues right after the warp kernel; 0: the warp kernel's
+    // last block finalises the cost
     int defer_cost;
     // 1: the 3D split path's warp, adjoint and gather kernels are launched
     // with programmatic stream serialisation (each may start while the one

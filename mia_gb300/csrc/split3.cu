@@ -523,8 +523,9 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             if (lane == 0) wsum[k][wy] = acc[k];
         }
     __syncthreads();
-    // an SSD cost the gather finalises needs no last-block pass here
-    const bool finalise_here = !(a.defer_cost && cost == 0);
+    // a deferred finalisation (the gather's for SSD, k_finalise3's for NCC)
+    // needs no last-block pass here
+    const bool finalise_here = !a.defer_cost;
     if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
@@ -1073,7 +1074,7 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     if (is_last) {
         __threadfence();
         __shared__ double red[GT3 / 32];
-        if (a.defer_cost) {
+        if (a.defer_cost && a.cost == 0) {
             // the SSD cost from the warp kernel's tile sums: the fixed-order
             // reduction of reduce_tile_sums (same striding, one component)
             const int ntw = a.ax[0].nt * a.ax[1].nt * a.ax[2].nt;
@@ -1140,6 +1141,19 @@ __global__ void MGR_ADJ_BOUNDS k_adjoint3(EvalArgs a)
 __global__ void MGR_GATHER_BOUNDS k_gather3(EvalArgs a, int with_gradient, int image_from_dense)
 {
     gather3_body(a, with_gradient, image_from_dense, blockIdx.x, gridDim.x);
+}
+
+// The NCC cost and force constants from the warp kernel's tile sums, one
+// block of NT3 threads: the reduction the warp kernel's last block makes
+// otherwise (same striding, same order), so that the warp blocks end
+// without a device-wide fence.  The adjoint kernel after it reads the
+// constants.
+__global__ void __launch_bounds__(NT3) k_finalise3(EvalArgs a)
+{
+    __shared__ double red[5 * (NT3 / 32)];
+    pdl_wait();
+    pdl_trigger();
+    reduce_tile_sums(a, a.ax[0].nt * a.ax[1].nt * a.ax[2].nt, size_t(a.n[0]) * a.n[1] * a.n[2], red);
 }
 
 __device__ __forceinline__ void decode_tile3(const EvalArgs &a, int t, int &bx, int &by, int &bz, int &nt)
@@ -1404,6 +1418,10 @@ void launch_warp3(const EvalArgs &a, cudaStream_t st)
     default: launch_warp3_z<16>(a, sm, st); break;
     }
     count_launch();
+    if (a.defer_cost && a.cost != MGR_COST_SSD) {
+        launch_pdl(a.pdl != 0, k_finalise3, dim3(1), dim3(NT3), 0, st, a);
+        count_launch();
+    }
 }
 
 void launch_adjoint3(const EvalArgs &a, cudaStream_t st)
