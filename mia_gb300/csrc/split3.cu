@@ -1073,26 +1073,25 @@ __device__ __forceinline__ void gather3_body(const EvalArgs &a, int with_gradien
     __syncthreads();
     if (is_last) {
         __threadfence();
-        __shared__ double red[GT3 / 32];
-        if (a.defer_cost && a.cost == 0) {
-            // the SSD cost from the warp kernel's tile sums: the fixed-order
-            // reduction of reduce_tile_sums (same striding, one component)
+        __shared__ double red[2 * (GT3 / 32)];
+        // v[0]: a deferred SSD cost from the warp kernel's tile sums (the
+        // fixed-order reduction of reduce_tile_sums: same striding, same
+        // tree); v[1]: the blocks' penalty partials; one pass for both
+        const bool fin = a.defer_cost && a.cost == 0;
+        double v2[2] = {0.0, 0.0};
+        if (fin) {
             const int ntw = a.ax[0].nt * a.ax[1].nt * a.ax[2].nt;
-            double tv[1] = {0.0};
-            for (int t = tid; t < ntw; t += GT3) tv[0] += ((volatile double *)a.tile_sums)[size_t(t) * 5];
-            block_sum<1>(tv, red);
-            if (tid == 0) {
-                const double s5[5] = {tv[0], 0.0, 0.0, 0.0, 0.0};
+            for (int t = tid; t < ntw; t += GT3) v2[0] += ((volatile double *)a.tile_sums)[size_t(t) * 5];
+        }
+        for (unsigned b = tid; b < unsigned(nblk); b += GT3) v2[1] += ((volatile double *)a.pen_part)[b];
+        block_sum<2>(v2, red);
+        if (tid == 0) {
+            if (fin) {
+                const double s5[5] = {v2[0], 0.0, 0.0, 0.0, 0.0};
                 finalise_cost(a, s5, size_t(a.n[0]) * a.n[1] * a.n[2]);
             }
-            __syncthreads();
-        }
-        double sv1[1] = {0.0};
-        for (unsigned b = tid; b < unsigned(nblk); b += GT3) sv1[0] += ((volatile double *)a.pen_part)[b];
-        block_sum<1>(sv1, red);
-        if (tid == 0) {
             double *sc = a.scalars;
-            const double pen = a.has_penalty ? sv1[0] : 0.0;
+            const double pen = a.has_penalty ? v2[1] : 0.0;
             sc[SC_PEN] = pen;
             sc[SC_COST_IMG] = a.cost_weight * sc[SC_VALUE];
             sc[SC_COST_PEN] = a.has_penalty ? a.pen_weight * pen : 0.0;
