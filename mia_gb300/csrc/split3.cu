@@ -196,9 +196,13 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             const float *c = C + r * FX + sx;
             Tx[r * 32 + lane] = fwx.x * c[0] + fwx.y * c[1] + fwx.z * c[2] + fwx.w * c[3];
         }
-        if (tid < RING_N) {   // one ring slot per lane of warp 0
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[tid])) : "memory");
-            rdone[tid] = 0;
+        // the ring's barriers: one thread initialises them all (mbarrier and
+        // bulk-copy instructions are issued by single threads here)
+        if (tid == 0) {
+            for (int k = 0; k < RING_N; ++k) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[k])) : "memory");
+                rdone[k] = 0;
+            }
             asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         }
     }
@@ -338,9 +342,11 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         nissued = ok ? min(boxs[4], RING_N) : 0;
     }
     __syncthreads();
-    // the box's first planes, one tensor copy per lane of warp 0 (the
-    // walk's waits on a plane end once its copy has been issued and landed)
-    if (wy == 0 && lane < nissued) issue_plane(lane);
+    // the box's first planes, issued by thread 0 after the barrier: the
+    // other warps start their walks meanwhile, their waits on a plane end
+    // once its copy has been issued and has landed
+    if (tid == 0)
+        for (int k = 0; k < nissued; ++k) issue_plane(k);
 
     const bool inxy = (x0 + lane < nx) && (y0 + wy < ny);
     const float px0 = float(x0 + lane), py0 = float(y0 + wy);

@@ -244,3 +244,22 @@ def test_batch_persistent_launch_equals_one_block_per_item(use_graphs):
     for (pb, cb, fb, nb), (pp, cp, fp, npp) in zip(base, pers):
         assert cb == cp and fb == fp and nb == npp
         assert np.array_equal(pb, pp)
+
+
+@pytest.mark.gpu
+def test_batch_persistent_launch_many_items_per_block():
+    """the persistent launches when each resident block draws several
+    (pair, tile) items (its shared-memory ring and barriers reused from one
+    item to the next): two SSD pairs of about a thousand tiles each against
+    the few hundred resident blocks of one GPU, bit for bit the results of
+    one block per item"""
+    from mia_gb300 import registration as R
+    shapes = [(192, 192, 128), (160, 144, 144)]
+    pairs = [_pair3d(171 + 7 * i, s) for i, s in enumerate(shapes)]
+    mg = R.minimizer("gsl", maxiter=3, step=0.1)
+    kw = dict(cost="ssd", penalty_weight=5.0)
+    base = R.register_batch(pairs, 8.0, 1, mg, **kw)
+    pers = R.register_batch(pairs, 8.0, 1, mg, persistent=True, **kw)
+    for (pb, cb, fb, nb), (pp, cp, fp, npp) in zip(base, pers):
+        assert cb == cp and fb == fp and nb == npp
+        assert np.array_equal(pb, pp)
