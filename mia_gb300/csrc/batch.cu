@@ -723,8 +723,8 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
         // host images on a device that reads pageable host memory
         // coherently (address translation through the host's page tables,
         // as on Grace-based systems): the normalisation kernels read the
-        // caller's arrays where they are, with no staged copy (the host path
-        // then costs two reads of the images over the CPU-GPU link);
+        // caller's arrays where they are, with no staged copy (one read of
+        // the images over the CPU-GPU link);
         // MGR_HOST_COPY=1 keeps the copies
         const bool direct = !images_on_device && coherent_host_access(device);
         trace_count("batch: images read in place (1 = yes)", direct ? 1.0 : 0.0);
@@ -762,7 +762,9 @@ mgr_status register_batch(int npairs, const mgr_level_desc *descs, int levels, c
                 ck(cudaStreamSynchronize(cudaStreamPerThread), "H2D sync");
             });
         }
-        const std::vector<char> varied = normalize_pairs(in_src, in_ref, nvox, out_src, out_ref, st);
+        // images read in place: the sums pass also copies them to the
+        // device, so that they cross the CPU-GPU link once
+        const std::vector<char> varied = normalize_pairs(in_src, in_ref, nvox, out_src, out_ref, st, direct);
         for (int p = 0; p < npairs; ++p) {
             PairRun &r = *pairs[p];
             r.src.release();   // the uploaded images are no longer read (stream-ordered free)

@@ -50,13 +50,21 @@ struct Wt4 {
 
 // per-block sums of a + b and a^2 + b^2 in double: block `blk` of `nblk`
 // takes elements blk * 256 + t + k * nblk * 256
+// ca, cb (optional): where the values read are also copied (host images
+// read in place are then read only once over the CPU-GPU link)
 __device__ __forceinline__ void pair_sums_body(const float *__restrict__ a, const float *__restrict__ b, size_t n,
-                                               double *part, int blk, int nblk)
+                                               double *part, int blk, int nblk, float *ca = nullptr,
+                                               float *cb = nullptr)
 {
     __shared__ double red[2 * 8];
     double v[2] = {0.0, 0.0};
     for (size_t i = blk * size_t(256) + threadIdx.x; i < n; i += size_t(nblk) * 256) {
-        const double fa = a[i], fb = b[i];
+        const float xa = a[i], xb = b[i];
+        if (ca) {
+            ca[i] = xa;
+            cb[i] = xb;
+        }
+        const double fa = xa, fb = xb;
         v[0] += fa + fb;
         v[1] += fa * fa + fb * fb;
     }
@@ -81,6 +89,7 @@ struct NormJob {
     size_t n;
     double *part;
     int nb, varied;
+    int copied;   // 1: the sums pass copied the images to src_out / ref_out; the map runs in place there
     double a, b;
 };
 
@@ -88,15 +97,16 @@ __global__ void __launch_bounds__(256) k_pair_sums_batch(const NormJob *jobs)
 {
     const NormJob &J = jobs[blockIdx.y];
     if (int(blockIdx.x) >= J.nb) return;
-    pair_sums_body(J.src, J.ref, J.n, J.part, blockIdx.x, J.nb);
+    pair_sums_body(J.src, J.ref, J.n, J.part, blockIdx.x, J.nb, J.copied ? J.src_out : nullptr,
+                   J.copied ? J.ref_out : nullptr);
 }
 
 __global__ void __launch_bounds__(256) k_apply_linear_batch(const NormJob *jobs)
 {
     const NormJob &J = jobs[blockIdx.y];
     if (!J.varied) return;
-    const float *in = blockIdx.z ? J.ref : J.src;
     float *out = blockIdx.z ? J.ref_out : J.src_out;
+    const float *in = J.copied ? out : (blockIdx.z ? J.ref : J.src);
     for (size_t i = blockIdx.x * size_t(256) + threadIdx.x; i < J.n; i += size_t(gridDim.x) * 256)
         out[i] = float(fma(J.a, double(in[i]), J.b));
 }
@@ -385,7 +395,7 @@ bool normalize_pair(const float *d_src, const float *d_ref, size_t n, float *d_s
 
 std::vector<char> normalize_pairs(const std::vector<const float *> &src, const std::vector<const float *> &ref,
                                   const std::vector<size_t> &n, const std::vector<float *> &src_out,
-                                  const std::vector<float *> &ref_out, cudaStream_t st)
+                                  const std::vector<float *> &ref_out, cudaStream_t st, bool copy_first)
 {
     const size_t np = src.size();
     std::vector<char> varied(np, 0);
@@ -404,6 +414,7 @@ std::vector<char> normalize_pairs(const std::vector<const float *> &src, const s
         J.n = n[i];
         J.nb = pair_sum_blocks(n[i]);
         J.varied = 0;
+        J.copied = copy_first ? 1 : 0;
         J.a = J.b = 0.0;
         nparts += size_t(J.nb) * 2;
         maxnb = std::max<size_t>(maxnb, J.nb);
