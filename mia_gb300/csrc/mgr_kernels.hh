@@ -133,6 +133,7 @@ void launch_gather_batch(int dim, const EvalArgs *args, const int2 *items, int n
 void launch_params_f32(const EvalArgs &a, cudaStream_t st);
 // (the batched driver's minimizer writes the float copy with each trial point)
 bool tile_supported3(int tx, int ty, int tz);
+bool tile_supported3_batch(int tx, int ty, int tz);
 size_t split3_smem(const EvalArgs &a, int which);
 void launch_warp3(const EvalArgs &a, cudaStream_t st);
 void launch_adjoint3(const EvalArgs &a, cudaStream_t st);

@@ -648,7 +648,7 @@ bool launch_split_batch(int dim, int tx, int ty, int tz, const EvalArgs *args, c
                         const int *active, size_t sm, int which, cudaStream_t st)
 {
     if (dim == 3) {
-        if (!tile_supported3(tx, ty, tz)) return false;
+        if (!tile_supported3_batch(tx, ty, tz)) return false;
         launch_split3_batch(tz, args, items, nitems, active, sm, which, st);
         return true;
     }

@@ -44,6 +44,8 @@
 #include "mgr_cost.cuh"
 #include "warp3_common.cuh"
 
+#include <type_traits>
+
 // the one-pair adjoint kernel: minimum resident blocks per SM (a cap of 40
 // registers, no spills) and the unroll factor of its plane walk (measured
 // at 192x192x128 SSD and 256^3 NCC against no unroll and no cap; the
@@ -382,15 +384,18 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
     }
     // the sample at plane t from the ring; ok = false when its taps are
     // not there (the voxel is deferred)
-    auto sample_ring = [&](int t, const float u[3], bool &ok) -> float {
+    auto sample_ring = [&](int t, int st, const float u[3], bool &ok) -> float {
         const int z = z0 + t;
         const float px = px0 - u[0], py = py0 - u[1], pz = float(z) - u[2];
         const int fx = ffloor16(px), fy = ffloor16(py), fz = ffloor16(pz);
-        const int col = fx - 1 - bxs, row = fy - 1 - bylo, kk = fz - 1 - bzbase;
+        const int col = fx - 1 - bxs, row = fy - 1 - bylo, dk = fz - 1 - bzbase - t;
         ok = ring_ok && unsigned(col) < unsigned(RING_X - 3) && unsigned(row) < unsigned(brows - 3) &&
-             unsigned(kk - t) < unsigned(span - 3);
-        if (ok)
-            return taps3_ring(ring, ring_slot(kk), row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
+             unsigned(dk) < unsigned(span - 3);
+        if (ok) {
+            // the slot of plane t + dk: st is plane t's, dk < RING_N
+            const int sl = st + dk >= RING_N ? st + dk - RING_N : st + dk;
+            return taps3_ring(ring, sl, row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
+        }
         return 0.0f;
     };
     auto add_cost = [&](float wv, float b) {
@@ -406,25 +411,29 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
             acc[4] += da * db;
         }
     };
-    auto release = [&](int t) {   // this warp is done with plane t
+    // this warp is done with planes t and t + 1 (t even: the pair's slots
+    // st, st + 1 share the counter of slot st); the last warp refills both
+    auto release = [&](int t, int st) {
         if (staged && t + RING_N < nplanes) {
             __syncwarp();
             if (lane == 0) {
-                const int slot = ring_slot(t);
                 __threadfence_block();
-                if (atomicAdd(&rdone[slot], 1u) == unsigned(NT3 / 32 - 1)) {
-                    rdone[slot] = 0;
+                if (atomicAdd(&rdone[st], 1u) == unsigned(NT3 / 32 - 1)) {
+                    rdone[st] = 0;
                     if (ring_ok && !ring_failed) {
                         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
                         issue_plane(t + RING_N);
-                        atomicAdd(&nissued, 1);
+                        const bool second = t + 1 + RING_N < nplanes;
+                        if (second) issue_plane(t + 1 + RING_N);
+                        atomicAdd(&nissued, second ? 2 : 1);
                     }
                 }
             }
         }
     };
     if (!staged && inxy) defer = ez >= 32 ? ~0u : (1u << ez) - 1u;
-    for (int t = 0; staged && t < ez; t += 2) {
+    static_assert(RING_N % 2 == 0, "the walk releases the ring's slots in pairs");
+    for (int t = 0, st = 0; staged && t < ez; t += 2, st = st + 2 == RING_N ? 0 : st + 2) {
         const bool two = t + 1 < ez;
         float ua[3], ub[3] = {0.0f, 0.0f, 0.0f};
         advance(t);
@@ -455,9 +464,9 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         }
         if (inxy) {
             bool oka, okb = true;
-            const float wa = sample_ring(t, ua, oka);
+            const float wa = sample_ring(t, st, ua, oka);
             float wb = 0.0f;
-            if (two) wb = sample_ring(t + 1, ub, okb);
+            if (two) wb = sample_ring(t + 1, st + 1, ub, okb);
             if (oka) {
                 wout[0] = wa;
                 add_cost(wa, r0);
@@ -479,8 +488,7 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         r3 = (inxy && t + 5 < ez) ? __ldg(rin + 5 * nxy) : 0.0f;
         wout += 2 * nxy;
         rin += 2 * nxy;
-        release(t);
-        if (two) release(t + 1);
+        release(t, st);
     }
     // the deferred voxels, in plane order: the displacement from the y
     // stage's window at plane t (the walk's values: the window then starts
@@ -1340,9 +1348,53 @@ size_t split3_smem(const EvalArgs &a, int which)
     return size_t(3) * Z.ac * TY3 * (TX3 + 1 + X.ac) * sizeof(float);
 }
 
+namespace {
+
+// the z-tile lengths the single-level kernels are compiled for:
+// fn(std::integral_constant<int, TZ>{}) for the length tz, false when tz is
+// not one of them.  The lengths between the powers of two let the
+// autotuner fit a level's tiles to the waves of resident blocks: 128 planes
+// in 20-plane tiles end with a row of 8-plane tiles that fills the last
+// wave's gaps, where 16-plane tiles leave half of the last wave idle.
+template <typename Fn>
+bool with_tz(int tz, Fn &&fn)
+{
+    switch (tz) {
+    case 4: fn(std::integral_constant<int, 4>{}); return true;
+    case 8: fn(std::integral_constant<int, 8>{}); return true;
+    case 12: fn(std::integral_constant<int, 12>{}); return true;
+    case 16: fn(std::integral_constant<int, 16>{}); return true;
+    case 20: fn(std::integral_constant<int, 20>{}); return true;
+    case 24: fn(std::integral_constant<int, 24>{}); return true;
+    case 32: fn(std::integral_constant<int, 32>{}); return true;
+    default: return false;
+    }
+}
+
+// the z-tile lengths of the batched and persistent kernels (the
+// registration drivers run 16-plane tiles)
+template <typename Fn>
+bool with_tz_batch(int tz, Fn &&fn)
+{
+    switch (tz) {
+    case 4: fn(std::integral_constant<int, 4>{}); return true;
+    case 8: fn(std::integral_constant<int, 8>{}); return true;
+    case 16: fn(std::integral_constant<int, 16>{}); return true;
+    case 32: fn(std::integral_constant<int, 32>{}); return true;
+    default: return false;
+    }
+}
+
+}  // namespace
+
 bool tile_supported3(int tx, int ty, int tz)
 {
-    return tx == TX3 && ty == TY3 && (tz == 4 || tz == 8 || tz == 16 || tz == 32);
+    return tx == TX3 && ty == TY3 && with_tz(tz, [](auto) {});
+}
+
+bool tile_supported3_batch(int tx, int ty, int tz)
+{
+    return tx == TX3 && ty == TY3 && with_tz_batch(tz, [](auto) {});
 }
 
 namespace {
@@ -1416,12 +1468,7 @@ void launch_warp3(const EvalArgs &a, cudaStream_t st)
 {
     launch_params_f32(a, st);
     const size_t sm = split3_smem(a, 0);
-    switch (a.ax[2].t) {
-    case 4: launch_warp3_z<4>(a, sm, st); break;
-    case 8: launch_warp3_z<8>(a, sm, st); break;
-    case 32: launch_warp3_z<32>(a, sm, st); break;
-    default: launch_warp3_z<16>(a, sm, st); break;
-    }
+    with_tz(a.ax[2].t, [&](auto z) { launch_warp3_z<decltype(z)::value>(a, sm, st); });
     count_launch();
     if (a.defer_cost && a.cost != MGR_COST_SSD) {
         launch_pdl(a.pdl != 0, k_finalise3, dim3(1), dim3(NT3), 0, st, a);
@@ -1432,12 +1479,7 @@ void launch_warp3(const EvalArgs &a, cudaStream_t st)
 void launch_adjoint3(const EvalArgs &a, cudaStream_t st)
 {
     const size_t sm = split3_smem(a, 1);
-    switch (a.ax[2].t) {
-    case 4: launch_adjoint3_z<4>(a, sm, st); break;
-    case 8: launch_adjoint3_z<8>(a, sm, st); break;
-    case 32: launch_adjoint3_z<32>(a, sm, st); break;
-    default: launch_adjoint3_z<16>(a, sm, st); break;
-    }
+    with_tz(a.ax[2].t, [&](auto z) { launch_adjoint3_z<decltype(z)::value>(a, sm, st); });
     count_launch();
 }
 
@@ -1454,45 +1496,27 @@ void launch_gather3(const EvalArgs &a, int with_gradient, int dense, cudaStream_
 
 void prepare_split3_batch(int tz, size_t sm_warp, size_t sm_adj)
 {
-    switch (tz) {
-    case 4: prepare3_z<4>(sm_warp, sm_adj); break;
-    case 8: prepare3_z<8>(sm_warp, sm_adj); break;
-    case 32: prepare3_z<32>(sm_warp, sm_adj); break;
-    default: prepare3_z<16>(sm_warp, sm_adj); break;
-    }
+    with_tz_batch(tz, [&](auto z) { prepare3_z<decltype(z)::value>(sm_warp, sm_adj); });
 }
 
 void launch_split3_batch(int tz, const EvalArgs *args, const int2 *items, int nitems, const int *active, size_t sm,
                          int which, cudaStream_t st)
 {
-    switch (tz) {
-    case 4: batch3_z<4>(args, items, nitems, active, sm, which, st); break;
-    case 8: batch3_z<8>(args, items, nitems, active, sm, which, st); break;
-    case 32: batch3_z<32>(args, items, nitems, active, sm, which, st); break;
-    default: batch3_z<16>(args, items, nitems, active, sm, which, st); break;
-    }
+    with_tz_batch(tz, [&](auto z) { batch3_z<decltype(z)::value>(args, items, nitems, active, sm, which, st); });
     count_launch();
 }
 
 int split3_queue_grid(int tz, int which, size_t sm)
 {
-    switch (tz) {
-    case 4: return queue_grid_z<4>(which, sm);
-    case 8: return queue_grid_z<8>(which, sm);
-    case 32: return queue_grid_z<32>(which, sm);
-    default: return queue_grid_z<16>(which, sm);
-    }
+    int g = 0;
+    with_tz_batch(tz, [&](auto z) { g = queue_grid_z<decltype(z)::value>(which, sm); });
+    return g;
 }
 
 void launch_split3_queue(int tz, const EvalArgs *args, const int2 *items, int nitems, const int *active, int *queue,
                          int grid, size_t sm, int which, cudaStream_t st)
 {
-    switch (tz) {
-    case 4: queue3_z<4>(args, items, nitems, active, queue, grid, sm, which, st); break;
-    case 8: queue3_z<8>(args, items, nitems, active, queue, grid, sm, which, st); break;
-    case 32: queue3_z<32>(args, items, nitems, active, queue, grid, sm, which, st); break;
-    default: queue3_z<16>(args, items, nitems, active, queue, grid, sm, which, st); break;
-    }
+    with_tz_batch(tz, [&](auto z) { queue3_z<decltype(z)::value>(args, items, nitems, active, queue, grid, sm, which, st); });
     count_launch();
 }
 

@@ -7,7 +7,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TILES = os.path.join(ROOT, "mia_gb300", "tiles.json")
-COMPILED3 = {(32, 8, 32), (32, 8, 16), (32, 8, 8), (32, 8, 4)}
+COMPILED3 = {(32, 8, 32), (32, 8, 24), (32, 8, 20), (32, 8, 16), (32, 8, 12), (32, 8, 8), (32, 8, 4)}
 COMPILED2 = {(32, 8, 1), (32, 16, 1), (64, 8, 1), (64, 16, 1), (32, 32, 1)}
 
 

@@ -224,7 +224,7 @@ def test_tiles_and_determinism():
     from mia_gb300 import synth
     p = synth.smooth_params(g.csize, 1.0, seed=3)
     ref_out = None
-    for tile in ((32, 8, 32), (32, 8, 16), (32, 8, 8), (32, 8, 4)):
+    for tile in ((32, 8, 32), (32, 8, 24), (32, 8, 20), (32, 8, 16), (32, 8, 12), (32, 8, 8), (32, 8, 4)):
         g.set_path("split", tile)
         out = g.evaluate(p)
         check_eval(g, o, o64, p, "split")
