@@ -240,9 +240,14 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         // thread's q values over the window range 0 .. zs[ez-1] + 3 with
         // non-negative weights summing to 1 (to less than 1 on the last
         // plane of the image, where 0 joins the range)
-        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float lo[3], hi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {   // the window's q values are kz = 0..3
+            lo[c] = fminf(fminf(q[c][0], q[c][1]), fminf(q[c][2], q[c][3]));
+            hi[c] = fmaxf(fmaxf(q[c][0], q[c][1]), fmaxf(q[c][2], q[c][3]));
+        }
         const int kend = zs[ez - 1] + 3;
-        for (int kz = 0; kz <= kend; ++kz)
+        for (int kz = 4; kz <= kend; ++kz)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float v = qat(c, kz);
@@ -625,7 +630,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
     float wm = (z0 > 0) ? __ldg(wc - nxy) : 0.0f;
     float w0 = __ldg(wc);
     __syncthreads();
-    const float k1 = fsc[0], k2 = fsc[1], ma = fsc[2], mb = fsc[3], fscale = fsc[4];
+    const float k1 = fsc[0], k2 = fsc[1], ma = fsc[2], mb = fsc[3], hscale = 0.5f * fsc[4];
 
     float acc[3][4];
 #pragma unroll
@@ -645,19 +650,15 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         if (inxy) {
             const float ym = __ldg(wc + ynm), yp = __ldg(wc + ynp);
             float g[3];
-            g[0] = bx_in ? 0.5f * (right - left) : 0.0f;
-            g[1] = by_in ? 0.5f * (yp - ym) : 0.0f;
-            g[2] = (z > 0 && z < nz - 1) ? 0.5f * (wp - wm) : 0.0f;
+            // central differences without their factor 1/2, which joins
+            // the force's scale
+            g[0] = bx_in ? right - left : 0.0f;
+            g[1] = by_in ? yp - ym : 0.0f;
+            g[2] = (z > 0 && z < nz - 1) ? wp - wm : 0.0f;
             const float b = __ldg(rc);
-            if (cost == 0) {
-                const float d = w0 - b;
+            const float s = cost == 0 ? (w0 - b) * hscale : 0.5f * (k1 * (k2 * (w0 - ma) - (b - mb)));
 #pragma unroll
-                for (int k = 0; k < 3; ++k) f[k] = (g[k] * d) * fscale;
-            } else {
-                const float s = k1 * (k2 * (w0 - ma) - (b - mb));
-#pragma unroll
-                for (int k = 0; k < 3; ++k) f[k] = s * g[k];
-            }
+            for (int k = 0; k < 3; ++k) f[k] = g[k] * s;
         }
         wc += nxy;
         rc += nxy;
@@ -705,7 +706,10 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         float *dst = Ax + e * AXc;
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
         int oc = 0;
-        for (int l = 0; l < ex; ++l) {
+        // all TX3 columns: the walk leaves 0 in the columns beyond the image,
+        // whose coefficient start is the last column's
+#pragma unroll 8
+        for (int l = 0; l < TX3; ++l) {
             const int o = asx[l];
             while (oc < o) {
                 dst[oc] = s0;
@@ -740,7 +744,9 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         const int pitch = AXc * 3;
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
         int oc = 0;
-        for (int yy = 0; yy < ey; ++yy) {
+#pragma unroll
+        for (int yy = 0; yy < TY3; ++yy) {
+            if (yy >= ey) break;
             const int o = asy[yy];
             while (oc < o) {
                 dst[oc * pitch] = s0;
