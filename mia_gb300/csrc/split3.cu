@@ -744,9 +744,7 @@ __device__ __forceinline__ void adjoint3_body(const EvalArgs &a, int bx, int by,
         const int pitch = AXc * 3;
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
         int oc = 0;
-#pragma unroll
-        for (int yy = 0; yy < TY3; ++yy) {
-            if (yy >= ey) break;
+        for (int yy = 0; yy < ey; ++yy) {
             const int o = asy[yy];
             while (oc < o) {
                 dst[oc * pitch] = s0;
