@@ -166,7 +166,9 @@ mgr_status mgr_level_force(mgr_level *lvl, const double *params, float *force,
 mgr_status mgr_level_translate(mgr_level *lvl, const float *force, double *grad);
 
 /* Select the evaluation strategy (MGR_PATH_*) and, for MGR_PATH_SPLIT, the
-   tile shape (0 = autotuned default).  Has no counterpart in the
+   tile shape (0 = autotuned default).  Compiled shapes: 3D 32 x 8 x TZ with
+   TZ in {4, 8, 12, 16, 20, 24, 32}; 2D 32 x 8, 32 x 16, 64 x 8, 64 x 16,
+   32 x 32; any other shape is MGR_ERR_ARG.  Has no counterpart in the
    reference: it chooses between implementations of the same result. */
 mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, int tile_z);
 

@@ -788,14 +788,18 @@ mgr_status mgr_level_set_path(mgr_level *lvl, int path, int tile_x, int tile_y, 
                 if (lvl->nc[k] - 3 > lvl->n[k] - 1)
                     throw std::invalid_argument("the fused path needs a coefficient spacing of at least one voxel");
         }
-        const bool fused_change = (path == MGR_PATH_FUSED) != (lvl->path == MGR_PATH_FUSED);
-        lvl->path = path;
+        // the shape is checked before anything changes: a refused call
+        // leaves the level as it was
         int t[3] = {tile_x > 0 ? tile_x : lvl->tile[0], tile_y > 0 ? tile_y : lvl->tile[1],
                     tile_z > 0 ? tile_z : lvl->tile[2]};
         if (lvl->d.dim == 2) t[2] = 1;
         if (!tile_supported(lvl->d.dim, t[0], t[1], t[2]))
-            throw std::invalid_argument("tile shape not compiled in (3D: 32x8x32, 32x8x16, 32x8x8, 32x8x4; "
+            throw std::invalid_argument("tile shape not compiled in (3D: 32x8xTZ, TZ in 4, 8, 12, 16, 20, 24, 32; "
                                         "2D: 32x8, 32x16, 64x8, 64x16, 32x32)");
+        if (!lvl->tile_fits(t, false))
+            throw std::invalid_argument("the tile's shared memory does not fit at this coefficient spacing");
+        const bool fused_change = (path == MGR_PATH_FUSED) != (lvl->path == MGR_PATH_FUSED);
+        lvl->path = path;
         bool changed = fused_change;
         for (int k = 0; k < 3; ++k)
             if (t[k] != lvl->tile[k]) {

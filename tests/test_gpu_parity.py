@@ -233,6 +233,14 @@ def test_tiles_and_determinism():
         again = g.evaluate(p)
         np.testing.assert_array_equal(out[4], again[4])   # bit-identical repeat
         assert rel_l2(out[4], ref_out[4]) < 1e-5
+    # a z length that is not compiled in is refused and the level keeps its tile
+    from mia_gb300 import _lib
+    for bad in ((32, 8, 7), (32, 8, 28), (16, 8, 16)):
+        with pytest.raises(_lib.MgrError) as e:
+            g.set_path("split", bad)
+        assert e.value.status == _lib.MGR_ERR_ARG
+    assert g.tile == (32, 8, 4)
+    check_eval(g, o, o64, p, "split")
 
 
 @pytest.mark.parametrize("cost", ["ssd", "ncc"])
