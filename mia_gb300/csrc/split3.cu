@@ -396,12 +396,13 @@ __device__ __forceinline__ void warp3_body(const EvalArgs &a, int bx, int by, in
         const int col = fx - 1 - bxs, row = fy - 1 - bylo, dk = fz - 1 - bzbase - t;
         ok = ring_ok && unsigned(col) < unsigned(RING_X - 3) && unsigned(row) < unsigned(brows - 3) &&
              unsigned(dk) < unsigned(span - 3);
-        if (ok) {
-            // the slot of plane t + dk: st is plane t's, dk < RING_N
-            const int sl = st + dk >= RING_N ? st + dk - RING_N : st + dk;
-            return taps3_ring(ring, sl, row, col, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
-        }
-        return 0.0f;
+        // a voxel whose taps are not in the ring reads the ring's first taps
+        // instead (the sample is discarded and the voxel deferred), so that
+        // no branch separates the step's two tap chains
+        const int c = ok ? col : 0, r = ok ? row : 0, d = ok ? dk : 0;
+        // the slot of plane t + d: st is plane t's, d < RING_N
+        const int sl = st + d >= RING_N ? st + d - RING_N : st + d;
+        return taps3_ring(ring, sl, r, c, px - float(fx), py - float(fy), pz - float(fz), mn, mxv);
     };
     auto add_cost = [&](float wv, float b) {
         if (cost == 0) {
